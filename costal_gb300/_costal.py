@@ -1,0 +1,316 @@
+"""Drop-in replacement of CosTaL 2.1.0's `costal._costal` extension module, on a GB300.
+
+Same functions, signatures, return types and error behaviour as the PyO3 module of
+crates/costal-py/src/lib.rs:80-465; the reference's pure-Python package (`costal._api`,
+`costal._leiden`) runs unchanged on top of it (INTEGRATION.md shows how to install it). Only type
+conversion and error mapping live here — as in lib.rs — and every computation is a call into
+libcostal_gb300.so: the kNN graph on the GPU, Leiden (the host consumer) in host C++.
+
+Differences from the reference, all documented:
+  - `matmul` names a coarse-pass backend of this library: "fp32" (default; "gemm" is accepted as
+    its alias) or "bf16" (certified split-BF16 tcgen05 tiles). Like the reference's backends they
+    change speed only, never the output. "accelerate" is Apple-only and unavailable here, as it is
+    for the reference on Linux.
+  - `row_block`, `col_block`, `sort_by_norm`, `prune` and `n_threads` are accepted and validated
+    but do not change the GPU tiling (the reference: they change speed only, knn.rs:39-44).
+  - k + margin above 128 raises NotImplementedError (the GPU keeps at most 128 candidates a row).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+__version__ = "2.1.0"
+
+NOT_CONTIGUOUS = "input must be a C-contiguous array; call np.ascontiguousarray first"  # lib.rs:35
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _arr(a, dtype, ndim, name="input"):
+    """PyReadonlyArray<T> extraction: exact dtype, C-contiguous (lib.rs:35, 68)."""
+    if not isinstance(a, np.ndarray):
+        raise TypeError(f"{name} must be a numpy.ndarray of {np.dtype(dtype).name}")
+    if a.dtype != np.dtype(dtype):
+        raise TypeError(f"{name} must have dtype {np.dtype(dtype).name}, got {a.dtype}")
+    if a.ndim != ndim:
+        raise TypeError(f"{name} must be {ndim}-dimensional, got {a.ndim}")
+    if not a.flags.c_contiguous:
+        raise ValueError(NOT_CONTIGUOUS)
+    return a
+
+
+def _call(fn, *args):
+    err, size = L.errbuf()
+    rc = fn(*args, err, size)
+    L.check(rc, err)
+
+
+def hello() -> str:
+    """crates/costal-core/src/lib.rs:23-25."""
+    return f"CosTaL core v{core_version()} is alive"
+
+
+def core_version() -> str:
+    return L.lib().costal_version().decode()
+
+
+def row_l2_norms(x):
+    """lib.rs:92-102: (n, d) float32 -> (n,) float32 row norms, on the GPU."""
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    out = np.empty(n, np.float32)
+    _call(L.lib().costal_row_l2_norms, _ptr(x), n, d, _ptr(out))
+    return out
+
+
+_SELECT_NAMES = ("cosine", "tanimoto")
+_BACKENDS = {None: L.BACKEND_FP32, "fp32": L.BACKEND_FP32, "gemm": L.BACKEND_FP32, "bf16": L.BACKEND_BF16}
+
+
+def _parse_select(select):
+    if select is None:
+        return "cosine"
+    if select not in _SELECT_NAMES:
+        raise ValueError(f'unknown select "{select}"')  # lib.rs:104-111
+    return select
+
+
+def _opts(select, margin, row_block, col_block, backend, sort_by_norm, prune, learned_prune=False):
+    o = L.KnnOpts()
+    o.margin = 0xFFFFFFFF if margin is None else int(margin)
+    o.select = L.SELECT[select]
+    o.backend = backend
+    o.row_block = int(row_block or 0)
+    o.col_block = int(col_block or 0)
+    o.sort_by_norm = int(bool(sort_by_norm))
+    o.prune = int(bool(prune))
+    o.learned_prune = int(bool(learned_prune))
+    return o
+
+
+def _check_knob(name, v):
+    if v is not None and int(v) < 0:
+        raise OverflowError(f"can't convert negative int to unsigned ({name})")
+
+
+def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None, matmul=None, sort_by_norm=True,
+               prune=True, n_threads=None):
+    """lib.rs:113-167: exact kNN. Returns ((idx int32 (n,k), cos float64 (n,k), norms float64 (n,)), stats)."""
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    if n > np.iinfo(np.int32).max:
+        raise ValueError(f"n={n} exceeds the int32 index range")
+    if matmul == "accelerate":
+        raise ValueError("matmul backend accelerate is not available on this platform")  # knn.rs:120-122
+    if matmul not in _BACKENDS:
+        raise ValueError(f'unknown matmul backend "{matmul}"')
+    for name, v in (("k", k), ("margin", margin), ("row_block", row_block), ("col_block", col_block),
+                    ("n_threads", n_threads)):
+        _check_knob(name, v)
+    sel = _parse_select(select)
+    k = int(k)
+    idx = np.empty((n, k), np.uint32)
+    cos = np.empty((n, k), np.float64)
+    norms = np.empty(n, np.float64)
+    st = L.KnnStats()
+    o = _opts(sel, margin, row_block, col_block, _BACKENDS[matmul], sort_by_norm, prune)
+    _call(L.lib().costal_knn_exact, _ptr(x), n, d, k, C.byref(o), _ptr(idx), _ptr(cos), _ptr(norms), C.byref(st))
+    stats = {
+        "fallback_rows": int(st.fallback_rows),
+        "row_block": int(st.row_block),
+        "col_block": int(st.col_block),
+        "matmul": "bf16" if matmul == "bf16" else ("gemm" if matmul == "gemm" else "fp32"),
+        "margin": int(st.margin),
+        "select": sel,
+        "blocks_skipped": int(st.blocks_skipped),
+        "blocks_total": int(st.blocks_total),
+        # GB300-only counters
+        "recomputed_rows": int(st.recomputed_rows),
+        "max_coarse_err": float(st.max_coarse_err),
+        "ms_total": float(st.ms_total),
+    }
+    return (idx.view(np.int32), cos, norms), stats
+
+
+def _knn_bruteforce(x, k, *, select=None, n_threads=None):
+    """lib.rs:169-191: every candidate in f64, no blocking (tests and benchmarks only)."""
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    _check_knob("k", k)
+    sel = _parse_select(select)
+    k = int(k)
+    idx = np.empty((n, k), np.uint32)
+    cos = np.empty((n, k), np.float64)
+    norms = np.empty(n, np.float64)
+    _call(L.lib().costal_knn_bruteforce, _ptr(x), n, d, k, L.SELECT[sel], _ptr(idx), _ptr(cos), _ptr(norms))
+    return idx.view(np.int32), cos, norms
+
+
+def _weight_code(weight):
+    if weight not in L.WEIGHT:
+        raise ValueError(f'unknown edge weight "{weight}"')  # lib.rs:202-203
+    return L.WEIGHT[weight]
+
+
+def _reweight(idx, cos, norms, weight):
+    """lib.rs:193-214: edge weights ("tanimoto" / "cosine" / "jaccard") on a kNN."""
+    w = _weight_code(weight)
+    idx = _arr(idx, np.int32, 2, "idx")
+    cos = _arr(cos, np.float64, 2, "cos")
+    norms = _arr(norms, np.float64, 1, "norms")
+    n, k = idx.shape
+    if cos.shape != (n, k) or norms.shape[0] != n:
+        raise ValueError("shapes of idx, cos and norms do not match")
+    out = np.empty((n, k), np.float64)
+    _call(L.lib().costal_reweight, n, k, _ptr(idx), _ptr(cos), _ptr(norms), w, _ptr(out))
+    return out
+
+
+def _fuzzy_union(idx, w):
+    """lib.rs:216-239: fuzzy-union symmetrisation -> upper-triangular (rows, cols, weights)."""
+    idx = _arr(idx, np.int32, 2, "idx")
+    w = _arr(w, np.float64, 2, "w")
+    n, k = idx.shape
+    if w.shape != (n, k):
+        raise ValueError("shapes of idx and w do not match")
+    rows = np.empty(n * k, np.int32)
+    cols = np.empty(n * k, np.int32)
+    wout = np.empty(n * k, np.float64)
+    m = C.c_uint64(0)
+    _call(L.lib().costal_fuzzy_union, n, k, _ptr(idx), _ptr(w), _ptr(rows), _ptr(cols), _ptr(wout), C.byref(m))
+    m = m.value
+    return rows[:m].copy(), cols[:m].copy(), wout[:m].copy()
+
+
+def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_knn=False):
+    """GB300 addition: the fused X -> kNN -> weights -> fuzzy union of _api.py:460-462 on the device.
+
+    Returns (rows int32, cols int32, weights float64), plus (idx, cos, norms) and stats when
+    return_knn is true. Bit-identical to calling _knn_exact, _reweight and _fuzzy_union in turn.
+    """
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    wc = _weight_code(weight)
+    if matmul not in _BACKENDS:
+        raise ValueError(f'unknown matmul backend "{matmul}"')
+    k = int(k)
+    rows = np.empty(n * k, np.int32)
+    cols = np.empty(n * k, np.int32)
+    wout = np.empty(n * k, np.float64)
+    m = C.c_uint64(0)
+    idx = cos = norms = None
+    if return_knn:
+        idx = np.empty((n, k), np.uint32)
+        cos = np.empty((n, k), np.float64)
+        norms = np.empty(n, np.float64)
+    st = L.KnnStats()
+    o = _opts("cosine", margin, None, None, _BACKENDS[matmul], True, True)
+    _call(L.lib().costal_build_graph, _ptr(x), n, d, k, C.byref(o), wc, _ptr(rows), _ptr(cols), _ptr(wout),
+          C.byref(m), _ptr(idx), _ptr(cos), _ptr(norms), C.byref(st))
+    m = m.value
+    edges = (rows[:m].copy(), cols[:m].copy(), wout[:m].copy())
+    if return_knn:
+        return edges, (idx.view(np.int32), cos, norms), st.as_dict()
+    return edges
+
+
+def _as_u32(a, name):
+    """lib.rs:241-249: a non-negative int32 array viewed as u32."""
+    a = _arr(a, np.int32, 1, name)
+    if a.size and a.min() < 0:
+        raise ValueError(f"negative index {int(a[a < 0][0])}")
+    return a.view(np.uint32)
+
+
+def _edges(rows, cols, weights):
+    r = _as_u32(rows, "rows")
+    c = _as_u32(cols, "cols")
+    w = _arr(weights, np.float64, 1, "weights")
+    if not (len(r) == len(c) == len(w)):
+        raise ValueError(f"edge arrays differ in length: {len(r)} rows, {len(c)} cols, {len(w)} weights")
+    return r, c, w
+
+
+def _u64(v, name):
+    v = int(v)
+    if v < 0:
+        raise OverflowError(f"can't convert negative int to unsigned ({name})")
+    return v
+
+
+def _leiden(n, rows, cols, weights, *, resolution, beta=0.01, n_iterations=2, seed=0, n_threads=None):
+    """lib.rs:272-306: Leiden (modularity) on an upper-triangular edge list.
+
+    Returns (membership int32, n_clusters, iterations, converged)."""
+    n = _u64(n, "n")
+    r, c, w = _edges(rows, cols, weights)
+    memb = np.empty(n, np.uint32)
+    ncl, it, conv = C.c_uint64(), C.c_uint64(), C.c_int()
+    _call(L.lib().costal_leiden, n, _ptr(r), _ptr(c), _ptr(w), len(w), 0, 0, float(resolution), float(beta),
+          int(n_iterations), _u64(seed, "seed"), None, _ptr(memb), C.byref(ncl), C.byref(it), C.byref(conv), None)
+    return memb.view(np.int32), int(ncl.value), int(it.value), bool(conv.value)
+
+
+def _leiden_many(n, rows, cols, weights, *, resolutions, seeds, beta=0.01, n_iterations=2, n_threads=None):
+    """lib.rs:308-350: Leiden at every (resolution, seed), resolutions outer -> int32 (runs, n)."""
+    n = _u64(n, "n")
+    r, c, w = _edges(rows, cols, weights)
+    res = np.ascontiguousarray([float(v) for v in resolutions], dtype=np.float64)
+    sd = np.ascontiguousarray([_u64(v, "seed") for v in seeds], dtype=np.uint64)
+    out = np.empty((len(res) * len(sd), n), np.uint32)
+    _call(L.lib().costal_leiden_many, n, _ptr(r), _ptr(c), _ptr(w), len(w), _ptr(res), len(res), _ptr(sd), len(sd),
+          float(beta), int(n_iterations), int(n_threads or 0), _ptr(out))
+    return out.view(np.int32)
+
+
+def _leiden_coo(n, rows, cols, weights, *, objective, resolution, beta, n_iterations, seed, initial=None,
+                n_threads=None):
+    """lib.rs:352-412: Leiden on an external COO list -> (labels int64, quality, n_clusters, iterations, converged)."""
+    if objective not in ("modularity", "cpm"):
+        raise ValueError(f"objective must be 'modularity' or 'cpm', got \"{objective}\"")
+    n = _u64(n, "n")
+    r = _arr(rows, np.uint32, 1, "rows")
+    c = _arr(cols, np.uint32, 1, "cols")
+    w = _arr(weights, np.float64, 1, "weights")
+    if not (len(r) == len(c) == len(w)):
+        raise ValueError(f"edge arrays differ in length: {len(r)} rows, {len(c)} cols, {len(w)} weights")
+    init = None if initial is None else _arr(initial, np.uint32, 1, "initial")
+    memb = np.empty(n, np.uint32)
+    ncl, it, conv, q = C.c_uint64(), C.c_uint64(), C.c_int(), C.c_double()
+    _call(L.lib().costal_leiden, n, _ptr(r), _ptr(c), _ptr(w), len(w), 0 if objective == "modularity" else 1, 1,
+          float(resolution), float(beta), int(n_iterations), _u64(seed, "seed"), _ptr(init), _ptr(memb),
+          C.byref(ncl), C.byref(it), C.byref(conv), C.byref(q))
+    return memb.astype(np.int64), float(q.value), int(ncl.value), int(it.value), bool(conv.value)
+
+
+def _modularity(n, rows, cols, weights, membership, resolution):
+    """lib.rs:414-428."""
+    n = _u64(n, "n")
+    r, c, w = _edges(rows, cols, weights)
+    m = _as_u32(membership, "membership")
+    q = C.c_double()
+    _call(L.lib().costal_modularity, n, _ptr(r), _ptr(c), _ptr(w), len(w), _ptr(m), float(resolution), C.byref(q))
+    return float(q.value)
+
+
+def l2_bytes_per_thread():
+    """lib.rs:430-434: the reference's CPU cache probe. The GPU kernels do not size tiles from a CPU
+    cache, so there is nothing to report (the reference also returns None when unavailable)."""
+    return None
+
+
+def tile_budget_bytes() -> int:
+    """lib.rs:436-440: the reference's fallback tile budget (the GPU tiles are fixed at 128 x 128)."""
+    return 1 << 20
+
+
+def default_matmul() -> str:
+    """lib.rs:442-446: name of the default coarse-pass backend."""
+    return "fp32"

@@ -1,0 +1,518 @@
+// The C ABI of libcostal_gb300: validation, the cached device context and the orchestration of the
+// kernels of knn_plain.cu, knn_tc.cu and graph.cu. Mirrors crates/costal-py/src/lib.rs (the PyO3
+// boundary) and the knn.rs/weight.rs/graph.rs entry points behind it; see include/costal_gb300.h.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "costal_gb300.h"
+#include "kernels.h"
+#include "knn_tc.h"
+
+namespace {
+
+using namespace costal;
+
+constexpr double F32_EPS = 1.1920928955078125e-07;  // 2^-23
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct Misc {  // small device-side results read back at the end of a call
+    unsigned long long bad_row;
+    unsigned long long max_err_bits;
+    unsigned long long first_bad_idx;
+    unsigned fb_count;
+    unsigned m;
+    unsigned tc_fail_count;
+    unsigned prune_fail_count;
+    unsigned long long blocks_skipped;
+    unsigned long long timeout_flag;
+};
+
+struct Context {
+    std::mutex mu;
+    bool inited = false;
+    int init_rc = COSTAL_OK;
+    std::string init_err;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    Misc* h_misc = nullptr;
+    DevBuf x, norms, xsT, cand_idx, cand_score, tau, out_idx, out_cos, out_w, fb_rows, fb_minsim, misc;
+    DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows;
+};
+
+Context& ctx() {
+    static Context c;
+    return c;
+}
+
+void put_err(char* err, size_t errlen, const std::string& msg) {
+    if (err && errlen) std::snprintf(err, errlen, "%s", msg.c_str());
+}
+
+cudaError_t ensure(DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 256;
+    if (b.bytes >= bytes) return cudaSuccess;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return e;
+    }
+    b.bytes = bytes;
+    return cudaSuccess;
+}
+
+struct Fail {
+    int rc;
+    std::string msg;
+};
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e__ = (call);                                                                       \
+        if (e__ != cudaSuccess) {                                                                       \
+            throw Fail{e__ == cudaErrorMemoryAllocation ? COSTAL_ENOMEM : COSTAL_ECUDA,                 \
+                       std::string(#call) + ": " + cudaGetErrorString(e__)};                            \
+        }                                                                                               \
+    } while (0)
+
+int init_locked(Context& c) {
+    if (c.inited) return c.init_rc;
+    c.inited = true;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        c.init_rc = COSTAL_ECUDA;
+        c.init_err = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        return c.init_rc;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p{};
+    cudaGetDeviceProperties(&p, dev);
+    if (!(p.major == 10 && p.minor == 3)) {
+        c.init_rc = COSTAL_ECUDA;
+        c.init_err = std::string("libcostal_gb300 is built for sm_103a (GB300); device 0 is ") + p.name + " sm_" +
+                     std::to_string(p.major) + std::to_string(p.minor);
+        return c.init_rc;
+    }
+    c.sm_count = p.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMallocHost(&c.h_misc, sizeof(Misc))) != cudaSuccess) {
+        c.init_rc = COSTAL_ECUDA;
+        c.init_err = std::string("context set-up failed: ") + cudaGetErrorString(e);
+        return c.init_rc;
+    }
+    for (auto& ev : c.ev) cudaEventCreate(&ev);
+    c.init_rc = COSTAL_OK;
+    return COSTAL_OK;
+}
+
+std::string knn_arg_error(uint64_t n, uint32_t k) {
+    if (n > 0xFFFFFFFFull) return "n=" + std::to_string(n) + " exceeds the u32 index range";  // knn.rs:118
+    if (k == 0 || (uint64_t)k >= n)
+        return "invalid k=" + std::to_string(k) + ": need 1 <= k <= n-1 (n=" + std::to_string(n) + ")";  // knn.rs:117
+    return "";
+}
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// The kNN on device buffers. Everything is asynchronous on `s` except the final read of Misc.
+// d_w (optional): the Tanimoto weight of every output edge, fused into the rescoring.
+void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn_opts& o, uint32_t* d_idx,
+             double* d_cos, double* d_norms, double* d_w, costal_knn_stats* st, cudaStream_t s) {
+    const uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
+    const int cap = (int)std::min<uint64_t>((uint64_t)k + margin, (uint64_t)n - 1);
+    const int dp = round_up(std::max(d, 1), 4);
+    const int np = round_up(n, 128);
+    if (coarse_slots(cap) == 0)
+        throw Fail{COSTAL_EUNSUPPORTED, "k + margin = " + std::to_string(k + margin) +
+                                            " exceeds the 128 candidates per row the GPU coarse pass keeps"};
+    CK(ensure(c.misc, sizeof(Misc)));
+    Misc* dm = c.misc.as<Misc>();
+    CK(cudaMemsetAsync(dm, 0, sizeof(Misc), s));
+    CK(cudaMemsetAsync(&dm->bad_row, 0xff, 8, s));
+    CK(ensure(c.xsT, (size_t)dp * np * 4));
+    CK(ensure(c.fb_rows, (size_t)n * 4));
+    CK(ensure(c.fb_minsim, (size_t)n * 8));
+    CK(cudaEventRecord(c.ev[0], s));
+    CK(launch_prep(d_x, n, d, np, dp, d_norms, c.xsT.as<float>(), &dm->bad_row, s));
+    CK(cudaEventRecord(c.ev[1], s));
+    const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
+    bool used_tc = false;
+    if (tanimoto) {
+        // Tanimoto selection (knn.rs:197-284): the exact f64 scan of every candidate on the GPU
+        // (knn.rs:884-924's brute force), which is exact by construction.
+        CK(cudaEventRecord(c.ev[2], s));
+        CK(cudaEventRecord(c.ev[3], s));
+        CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, nullptr, nullptr, nullptr, 1, 1,
+                         std::min(n, 8 * c.sm_count), d_idx, d_cos, d_w, s));
+    } else {
+        CK(ensure(c.cand_idx, (size_t)n * cap * 4));
+        CK(ensure(c.cand_score, (size_t)n * cap * 4));
+        CK(ensure(c.tau, (size_t)n * 4));
+        const double eps = ((double)d + 4.0) * F32_EPS;  // knn.rs:185-187
+        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap)) {
+            used_tc = true;
+            CK(ensure(c.tc_ws, tc::workspace_bytes(n, d)));
+            CK(ensure(c.tc_rows, (size_t)n * 4));
+            tc::Plan plan{};
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, s, plan));
+            CK(tc::launch_coarse(plan, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(),
+                                 &dm->timeout_flag, c.sm_count, s));
+            CK(cudaEventRecord(c.ev[2], s));
+            // The split-BF16 certificate with its per-row bound; rows that fail it are listed in
+            // tc_rows, re-run by the FP32 coarse kernel and rescored with the FP32 bound, whose
+            // failures in turn take the full-row regather.
+            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                              c.tau.as<float>(), d_norms, plan.row_eps, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx,
+                              d_cos, d_w, c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
+                              &dm->max_err_bits, s));
+            if (dp > 64 || coarse_fp32_smem(dp, cap) > 227 * 1024)
+                throw Fail{COSTAL_EUNSUPPORTED, "d too large for the FP32 re-run of uncertified rows"};
+            CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, c.tc_rows.as<uint32_t>(), &dm->tc_fail_count,
+                                  c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
+            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                              c.tau.as<float>(), d_norms, nullptr, eps, cap < n - 1, 0, c.tc_rows.as<uint32_t>(),
+                              &dm->tc_fail_count, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
+                              &dm->fb_count, nullptr, s));
+            CK(cudaEventRecord(c.ev[3], s));
+        } else {
+            if (dp > 64)
+                throw Fail{COSTAL_EUNSUPPORTED, "d > 64 is not supported by the FP32 coarse kernel yet"};
+            if (coarse_fp32_smem(dp, cap) > 227 * 1024)
+                throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 coarse kernel"};
+            CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, nullptr, nullptr, c.cand_idx.as<uint32_t>(),
+                                  c.cand_score.as<float>(), c.tau.as<float>(), s));
+            CK(cudaEventRecord(c.ev[2], s));
+            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                              c.tau.as<float>(), d_norms, nullptr, eps, cap < n - 1, 0, nullptr, nullptr, d_idx,
+                              d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->fb_count,
+                              &dm->max_err_bits, s));
+            CK(cudaEventRecord(c.ev[3], s));
+        }
+        if (cap < n - 1) {
+            if (gather_smem(k, d, dp) > 227 * 1024)
+                throw Fail{COSTAL_EUNSUPPORTED, "k too large for the GPU regather kernel"};
+            CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, c.fb_rows.as<uint32_t>(),
+                             c.fb_minsim.as<double>(), &dm->fb_count, 0, 0, std::min(n, 4 * c.sm_count), d_idx,
+                             d_cos, d_w, s));
+        }
+    }
+    CK(cudaEventRecord(c.ev[4], s));
+    CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const Misc& hm = *c.h_misc;
+    if (hm.bad_row != ~0ull) throw Fail{COSTAL_EINVAL, "row " + std::to_string(hm.bad_row) + " contains NaN or inf"};
+    if (hm.timeout_flag) throw Fail{COSTAL_ETIMEOUT, "a bounded device wait in the tensor-core kernel gave up"};
+    if (st) {
+        st->fallback_rows = hm.fb_count;
+        st->row_block = 128;
+        st->col_block = used_tc ? (uint64_t)tc::BLOCK_N : 128;
+        st->blocks_skipped = hm.blocks_skipped;
+        st->blocks_total = (uint64_t)((n + 127) / 128) * (uint64_t)((n + st->col_block - 1) / st->col_block);
+        st->margin = margin;
+        st->recomputed_rows = used_tc ? hm.tc_fail_count : 0;
+        st->pruned_fallback_rows = hm.prune_fail_count;
+        double me;
+        std::memcpy(&me, &hm.max_err_bits, 8);
+        st->max_coarse_err = me;
+        st->ms_prep = elapsed(c.ev[0], c.ev[1]);
+        st->ms_coarse = elapsed(c.ev[1], c.ev[2]);
+        st->ms_rescore = elapsed(c.ev[2], c.ev[3]);
+        st->ms_fallback = elapsed(c.ev[3], c.ev[4]);
+        st->ms_total = elapsed(c.ev[0], c.ev[4]);
+    }
+}
+
+costal_knn_opts defaults() {
+    costal_knn_opts o{};
+    o.margin = UINT32_MAX;
+    o.select = COSTAL_SELECT_COSINE;
+    o.backend = COSTAL_BACKEND_FP32;
+    o.sort_by_norm = 1;
+    o.prune = 1;
+    return o;
+}
+
+template <class F>
+int guarded(char* err, size_t errlen, F&& f) {
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lock(c.mu);
+    int rc = init_locked(c);
+    if (rc != COSTAL_OK) {
+        put_err(err, errlen, c.init_err);
+        return rc;
+    }
+    try {
+        f(c);
+    } catch (const Fail& fl) {
+        put_err(err, errlen, fl.msg);
+        return fl.rc;
+    } catch (const std::exception& ex) {
+        put_err(err, errlen, ex.what());
+        return COSTAL_ECUDA;
+    }
+    return COSTAL_OK;
+}
+
+void check_knn_args(uint64_t n, uint32_t d, uint32_t k) {
+    std::string m = knn_arg_error(n, k);
+    if (!m.empty()) throw Fail{COSTAL_EINVAL, m};
+    if (n > (uint64_t)INT32_MAX) throw Fail{COSTAL_EINVAL, "n=" + std::to_string(n) + " exceeds the int32 index range"};
+    if ((uint64_t)n * k > (uint64_t)INT32_MAX)
+        throw Fail{COSTAL_EUNSUPPORTED, "n*k exceeds the int32 edge index range of the GPU path"};
+    (void)d;
+}
+
+// Check an (n, k) neighbour matrix on the device: lib.rs:65-78 reports the first bad value.
+void check_neighbours(Context& c, const int32_t* d_idx, const int32_t* h_idx, uint64_t n, uint32_t k, cudaStream_t s) {
+    CK(ensure(c.misc, sizeof(Misc)));
+    Misc* dm = c.misc.as<Misc>();
+    CK(cudaMemsetAsync(&dm->first_bad_idx, 0xff, 8, s));
+    CK(launch_check_idx(d_idx, n * k, (int)n, &dm->first_bad_idx, s));
+    CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (c.h_misc->first_bad_idx != ~0ull) {
+        int32_t bad = h_idx[c.h_misc->first_bad_idx];
+        throw Fail{COSTAL_EINVAL, "neighbor index " + std::to_string(bad) + " out of range (n=" + std::to_string(n) + ")"};
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* costal_version(void) { return "2.1.0"; }
+
+int costal_device_ok(char* err, size_t errlen) {
+    return guarded(err, errlen, [](Context&) {});
+}
+
+int costal_row_l2_norms(const float* x, uint64_t n, uint32_t d, float* out, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (n == 0) return;
+        cudaStream_t s = c.stream;
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.f32out, n * 4ull));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        CK(launch_row_l2_norms_f32(c.x.as<float>(), (int)n, (int)d, c.f32out.as<float>(), s));
+        CK(cudaMemcpyAsync(out, c.f32out.p, n * 4ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_knn_exact(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts, uint32_t* idx,
+                     double* cos, double* norms, costal_knn_stats* stats, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = c.stream;
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.out_idx, n * k * 4ull));
+        CK(ensure(c.out_cos, n * k * 8ull));
+        CK(ensure(c.norms, n * 8ull));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        run_knn(c, c.x.as<float>(), (int)n, (int)d, (int)k, o, c.out_idx.as<uint32_t>(), c.out_cos.as<double>(),
+                c.norms.as<double>(), nullptr, stats, s);
+        CK(cudaMemcpyAsync(idx, c.out_idx.p, n * k * 4ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(cos, c.out_cos.p, n * k * 8ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(norms, c.norms.p, n * 8ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_knn_exact_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                            uint32_t* d_idx, double* d_cos, double* d_norms, costal_knn_stats* stats, void* stream,
+                            char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+        run_knn(c, d_x, (int)n, (int)d, (int)k, o, d_idx, d_cos, d_norms, nullptr, stats, s);
+    });
+}
+
+int costal_knn_bruteforce(const float* x, uint64_t n, uint32_t d, uint32_t k, uint32_t select, uint32_t* idx,
+                          double* cos, double* norms, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        cudaStream_t s = c.stream;
+        const int dp = round_up(std::max((int)d, 1), 4), np = round_up((int)n, 128);
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.out_idx, n * k * 4ull));
+        CK(ensure(c.out_cos, n * k * 8ull));
+        CK(ensure(c.norms, n * 8ull));
+        CK(ensure(c.xsT, (size_t)dp * np * 4));
+        CK(ensure(c.misc, sizeof(Misc)));
+        Misc* dm = c.misc.as<Misc>();
+        CK(cudaMemsetAsync(&dm->bad_row, 0xff, 8, s));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        CK(launch_prep(c.x.as<float>(), (int)n, (int)d, np, dp, c.norms.as<double>(), c.xsT.as<float>(), &dm->bad_row, s));
+        if (gather_smem(k, d, dp) > 227 * 1024) throw Fail{COSTAL_EUNSUPPORTED, "k too large for the GPU scan kernel"};
+        CK(launch_gather(c.x.as<float>(), c.xsT.as<float>(), (int)n, np, (int)d, dp, (int)k, c.norms.as<double>(),
+                         nullptr, nullptr, nullptr, 1, select == COSTAL_SELECT_TANIMOTO ? 1 : 0,
+                         std::min((int)n, 8 * c.sm_count), c.out_idx.as<uint32_t>(), c.out_cos.as<double>(), nullptr, s));
+        CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(idx, c.out_idx.p, n * k * 4ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(cos, c.out_cos.p, n * k * 8ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(norms, c.norms.p, n * 8ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (c.h_misc->bad_row != ~0ull)
+            throw Fail{COSTAL_EINVAL, "row " + std::to_string(c.h_misc->bad_row) + " contains NaN or inf"};
+    });
+}
+
+int costal_reweight(uint64_t n, uint32_t k, const int32_t* idx, const double* cos, const double* norms, uint32_t weight,
+                    double* out, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (weight > COSTAL_WEIGHT_JACCARD) throw Fail{COSTAL_EINVAL, "unknown edge weight"};
+        const uint64_t nk = n * k;
+        if (nk == 0) return;
+        if (nk > (uint64_t)INT32_MAX) throw Fail{COSTAL_EUNSUPPORTED, "n*k exceeds the int32 range of the GPU path"};
+        cudaStream_t s = c.stream;
+        CK(ensure(c.idx_in, nk * 4));
+        CK(ensure(c.cos_in, nk * 8));
+        CK(ensure(c.norms_in, n * 8));
+        CK(ensure(c.w_in, nk * 8));
+        CK(cudaMemcpyAsync(c.idx_in.p, idx, nk * 4, cudaMemcpyHostToDevice, s));
+        check_neighbours(c, c.idx_in.as<int32_t>(), idx, n, k, s);
+        if (weight == COSTAL_WEIGHT_COSINE) {
+            std::memcpy(out, cos, nk * 8);  // weight.rs:51: the rescored cosine itself
+            return;
+        }
+        if (weight == COSTAL_WEIGHT_TANIMOTO) {
+            CK(cudaMemcpyAsync(c.cos_in.p, cos, nk * 8, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(c.norms_in.p, norms, n * 8, cudaMemcpyHostToDevice, s));
+            CK(launch_tanimoto_w(c.idx_in.as<uint32_t>(), c.cos_in.as<double>(), c.norms_in.as<double>(), nk, (int)k,
+                                 c.w_in.as<double>(), s));
+        } else {
+            CK(ensure(c.jac, nk * 4));
+            CK(launch_jaccard(c.idx_in.as<uint32_t>(), (int)n, (int)k, c.jac.as<uint32_t>(), c.w_in.as<double>(), s));
+        }
+        CK(cudaMemcpyAsync(out, c.w_in.p, nk * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+namespace {
+void run_union(Context& c, const uint32_t* d_idx, const double* d_w, uint64_t n, uint32_t k, int32_t* d_rows,
+               int32_t* d_cols, double* d_wout, uint64_t* m, cudaStream_t s) {
+    CK(ensure(c.fu_scratch, fuzzy_union_scratch_bytes((int)n, (int)k)));
+    CK(ensure(c.misc, sizeof(Misc)));
+    Misc* dm = c.misc.as<Misc>();
+    CK(launch_fuzzy_union(d_idx, d_w, (int)n, (int)k, c.fu_scratch.p, d_rows, d_cols, d_wout, &dm->m, s));
+    CK(cudaMemcpyAsync(&c.h_misc->m, &dm->m, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *m = c.h_misc->m;
+}
+}  // namespace
+
+int costal_fuzzy_union(uint64_t n, uint32_t k, const int32_t* idx, const double* w, int32_t* rows, int32_t* cols,
+                       double* w_out, uint64_t* m, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        *m = 0;
+        const uint64_t nk = n * k;
+        if (nk == 0) return;
+        if (nk > (uint64_t)INT32_MAX) throw Fail{COSTAL_EUNSUPPORTED, "n*k exceeds the int32 range of the GPU path"};
+        cudaStream_t s = c.stream;
+        CK(ensure(c.idx_in, nk * 4));
+        CK(ensure(c.w_in, nk * 8));
+        CK(ensure(c.rows, nk * 4));
+        CK(ensure(c.cols, nk * 4));
+        CK(ensure(c.wout, nk * 8));
+        CK(cudaMemcpyAsync(c.idx_in.p, idx, nk * 4, cudaMemcpyHostToDevice, s));
+        check_neighbours(c, c.idx_in.as<int32_t>(), idx, n, k, s);
+        CK(cudaMemcpyAsync(c.w_in.p, w, nk * 8, cudaMemcpyHostToDevice, s));
+        run_union(c, c.idx_in.as<uint32_t>(), c.w_in.as<double>(), n, k, c.rows.as<int32_t>(), c.cols.as<int32_t>(),
+                  c.wout.as<double>(), m, s);
+        CK(cudaMemcpyAsync(rows, c.rows.p, *m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(cols, c.cols.p, *m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(w_out, c.wout.p, *m * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+namespace {
+// X (device) -> kNN -> weights -> fuzzy union, all on the device.
+void run_build(Context& c, const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts& o,
+               uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m, costal_knn_stats* st,
+               cudaStream_t s) {
+    if (weight > COSTAL_WEIGHT_JACCARD) throw Fail{COSTAL_EINVAL, "unknown edge weight"};
+    const uint64_t nk = n * k;
+    CK(ensure(c.out_idx, nk * 4));
+    CK(ensure(c.out_cos, nk * 8));
+    CK(ensure(c.norms, n * 8));
+    CK(ensure(c.out_w, nk * 8));
+    double* fused_w = weight == COSTAL_WEIGHT_TANIMOTO ? c.out_w.as<double>() : nullptr;
+    run_knn(c, d_x, (int)n, (int)d, (int)k, o, c.out_idx.as<uint32_t>(), c.out_cos.as<double>(), c.norms.as<double>(),
+            fused_w, st, s);
+    const double* wsrc = c.out_w.as<double>();
+    if (weight == COSTAL_WEIGHT_COSINE) {
+        wsrc = c.out_cos.as<double>();
+    } else if (weight == COSTAL_WEIGHT_JACCARD) {
+        CK(ensure(c.jac, nk * 4));
+        CK(launch_jaccard(c.out_idx.as<uint32_t>(), (int)n, (int)k, c.jac.as<uint32_t>(), c.out_w.as<double>(), s));
+    }
+    run_union(c, c.out_idx.as<uint32_t>(), wsrc, n, k, d_rows, d_cols, d_w, m, s);
+}
+}  // namespace
+
+int costal_build_graph(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts, uint32_t weight,
+                       int32_t* rows, int32_t* cols, double* w, uint64_t* m, uint32_t* idx, double* cos, double* norms,
+                       costal_knn_stats* stats, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = c.stream;
+        const uint64_t nk = n * k;
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.rows, nk * 4));
+        CK(ensure(c.cols, nk * 4));
+        CK(ensure(c.wout, nk * 8));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        run_build(c, c.x.as<float>(), n, d, k, o, weight, c.rows.as<int32_t>(), c.cols.as<int32_t>(),
+                  c.wout.as<double>(), m, stats, s);
+        CK(cudaMemcpyAsync(rows, c.rows.p, *m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(cols, c.cols.p, *m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(w, c.wout.p, *m * 8, cudaMemcpyDeviceToHost, s));
+        if (idx) CK(cudaMemcpyAsync(idx, c.out_idx.p, nk * 4, cudaMemcpyDeviceToHost, s));
+        if (cos) CK(cudaMemcpyAsync(cos, c.out_cos.p, nk * 8, cudaMemcpyDeviceToHost, s));
+        if (norms) CK(cudaMemcpyAsync(norms, c.norms.p, n * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                              uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m,
+                              costal_knn_stats* stats, void* stream, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+        run_build(c, d_x, n, d, k, o, weight, d_rows, d_cols, d_w, m, stats, s);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+// Shared device helpers of the GB300 kNN-graph kernels (sm_103a only).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define COSTAL_FULL_MASK 0xffffffffu
+
+namespace costal {
+
+// ---- exact f64 arithmetic in the reference's order of operations ---------------------------------
+//
+// Each helper names the rounding of every operation, so nvcc can never contract a multiply and an
+// add into one FMA where the reference (Rust, which never contracts) rounds twice.
+
+// knn.rs:290-296 `dot64`: Σ_t f64(a_t)·f64(b_t) in dimension order. An f32×f32 product is exact
+// in f64, so fma(a, b, s) rounds exactly like s + a·b: the FMA is bit-identical here.
+__device__ __forceinline__ double dot64_step(double s, float a, float b) {
+    return __fma_rn((double)a, (double)b, s);
+}
+
+// knn.rs:301-312 `cos64`: 0 for a zero row, dot / (n_i·n_j), −0 → +0.
+__device__ __forceinline__ double cos64(double dot, double ni, double nj) {
+    if (ni == 0.0 || nj == 0.0) return 0.0;
+    double c = __ddiv_rn(dot, __dmul_rn(ni, nj));
+    return c == 0.0 ? 0.0 : c;
+}
+
+// weight.rs:30-37 `tani_from_cos`: d = a·b·cos; 0 when d == 0, else d / (a² + b² − d).
+__device__ __forceinline__ double tani_from_cos(double a, double b, double c) {
+    double d = __dmul_rn(__dmul_rn(a, b), c);
+    if (d == 0.0) return 0.0;
+    double den = __dsub_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), d);
+    return __ddiv_rn(d, den);
+}
+
+// Rust's f64::total_cmp as a signed integer key (knn.rs:589-591 sorts with it).
+__device__ __forceinline__ long long total_key(double v) {
+    long long b = __double_as_longlong(v);
+    return b ^ (long long)(((unsigned long long)(b >> 63)) >> 1);
+}
+
+// (score desc, index asc): the final order of a row (knn.rs:589-591).
+__device__ __forceinline__ bool before64(double sa, uint32_t ia, double sb, uint32_t ib) {
+    long long ka = total_key(sa), kb = total_key(sb);
+    return ka > kb || (ka == kb && ia < ib);
+}
+
+// ---- cp.async (Ampere-style asynchronous global→shared copies; no spin-waits) -------------------
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+}  // namespace costal

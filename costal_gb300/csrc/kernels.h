@@ -1,0 +1,41 @@
+// Internal launcher declarations shared by the .cu files of libcostal_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace costal {
+
+// ---- knn_plain.cu ------------------------------------------------------------------------------
+cudaError_t launch_prep(const float* x, int n, int d, int np, int dp, double* norms, float* xsT,
+                        unsigned long long* bad_row, cudaStream_t st);
+cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cudaStream_t st);
+int coarse_slots(int cap);
+size_t coarse_fp32_smem(int dp, int cap);
+// qlist/qcount (optional): run only the rows listed on the device (128 per CTA, grid sized for n).
+cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                               const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
+                               cudaStream_t st);
+cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
+                           const float* cand_score, const float* tau, const double* norms, const double* row_eps,
+                           double eps, int certify, int select, const uint32_t* rlist, const unsigned* rcount,
+                           uint32_t* out_idx, double* out_cos, double* out_w, uint32_t* fb_rows, double* fb_minsim,
+                           unsigned* fb_count, unsigned long long* max_err_bits, cudaStream_t st);
+int gather_capb(int k);
+size_t gather_smem(int k, int d, int dp);
+cudaError_t launch_gather(const float* x, const float* xsT, int n, int np, int d, int dp, int k, const double* norms,
+                          const uint32_t* rows, const double* minsim, const unsigned* count, int all_rows, int select,
+                          int grid, uint32_t* out_idx, double* out_cos, double* out_w, cudaStream_t st);
+
+// ---- graph.cu ----------------------------------------------------------------------------------
+cudaError_t launch_check_idx(const int32_t* idx, uint64_t nk, int n, unsigned long long* first_bad, cudaStream_t st);
+cudaError_t launch_tanimoto_w(const uint32_t* idx, const double* cos, const double* norms, uint64_t nk, int k,
+                              double* out, cudaStream_t st);
+cudaError_t launch_jaccard(const uint32_t* idx, int n, int k, uint32_t* sorted_scratch, double* out, cudaStream_t st);
+// Fuzzy union S + Sᵀ − S∘Sᵀ on the device. Scratch sizes in fuzzy_union_scratch_bytes.
+size_t fuzzy_union_scratch_bytes(int n, int k);
+cudaError_t launch_fuzzy_union(const uint32_t* idx, const double* w, int n, int k, void* scratch, int32_t* rows,
+                               int32_t* cols, double* w_out, uint32_t* m_dev, cudaStream_t st);
+
+}  // namespace costal

@@ -1,0 +1,670 @@
+// Plain FP32 exact kNN on GB300: the correctness-defining form of the hot path.
+//
+// Restates the algorithm of crates/costal-core/src/knn.rs (CosTaL 2.1.0) for one GPU:
+//   k_prep      — knn.rs:315-323 row_norms64 (f64, dimension order) and knn.rs:420-436 the
+//                 L2-normalised f32 working copy, written transposed (d_pad × n_pad) for the tiles;
+//                 also knn.rs:325-342's non-finite check (first bad row).
+//   k_coarse    — knn.rs:603-660 + 758-875: every (query block × column tile) dot product in FP32
+//                 on the CUDA cores (tiles staged in shared memory by cp.async), fused with the
+//                 per-query top-cap selection by (score desc, index asc).
+//   k_rescore   — knn.rs:688-720 + 746-753: f64 rescoring of the cap candidates, the sort, the
+//                 ε-certificate s_k > τ + (d+4)·2⁻²³, and (fused) the Tanimoto edge weight of
+//                 weight.rs:30-37 for the k survivors.
+//   k_gather    — knn.rs:723-743: the full-row regather for rows that fail the certificate; with
+//                 min_sim = −∞ over every row it is knn.rs:884-924's brute force.
+//
+// The output does not depend on how the coarse pass orders its sums: every candidate left out has
+// an FP32 score ≤ τ, its exact score is within ε of it, and the certificate (or the regather)
+// makes the final ranking a function of the f64 rescoring alone (knn.rs:682-687).
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace costal {
+
+// =================================================================================================
+// k_prep: norms, non-finite check, transposed normalised copy
+// =================================================================================================
+
+constexpr int PREP_ROWS = 128;
+constexpr int PREP_TCHUNK = 64;
+
+// Block = PREP_ROWS threads = PREP_ROWS rows. Rows are staged through shared memory in chunks of
+// PREP_TCHUNK dimensions (coalesced loads), then each thread walks its own row in dimension order,
+// so the f64 sum has exactly the reference's order.
+__global__ void __launch_bounds__(PREP_ROWS) k_prep(const float* __restrict__ x, int n, int d, int np, int dp,
+                                                    double* __restrict__ norms, float* __restrict__ xsT,
+                                                    unsigned long long* __restrict__ bad_row) {
+    __shared__ float tile[PREP_ROWS * (PREP_TCHUNK + 1)];
+    const int r0 = blockIdx.x * PREP_ROWS;
+    const int r = r0 + threadIdx.x;
+    const int rows = min(PREP_ROWS, n - r0);
+    double s = 0.0;
+    bool bad = false;
+    for (int t0 = 0; t0 < d; t0 += PREP_TCHUNK) {
+        const int tc = min(PREP_TCHUNK, d - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < rows * tc; e += PREP_ROWS) {
+            const int rr = e / tc, tt = e % tc;
+            tile[rr * (PREP_TCHUNK + 1) + tt] = x[(size_t)(r0 + rr) * d + t0 + tt];
+        }
+        __syncthreads();
+        if (r < n) {
+            for (int tt = 0; tt < tc; ++tt) {
+                const float v = tile[threadIdx.x * (PREP_TCHUNK + 1) + tt];
+                bad |= !isfinite(v);
+                s = dot64_step(s, v, v);
+            }
+        }
+    }
+    double nrm = __dsqrt_rn(s);
+    if (r < n) {
+        norms[r] = nrm;
+        if (bad) atomicMin(bad_row, (unsigned long long)r);
+    }
+    // xs = f32(x / ‖x‖) through the f64 reciprocal: ≤ 2⁻²⁴(1 + 2⁻²⁸) relative error per entry,
+    // inside the (d+4)·2⁻²³ coarse bound the certificate uses. Zero rows stay zero (knn.rs:430-435).
+    const double inv = (r < n && nrm > 0.0) ? __drcp_rn(nrm) : 0.0;
+    for (int t0 = 0; t0 < dp; t0 += PREP_TCHUNK) {
+        const int tc = min(PREP_TCHUNK, d - t0);
+        if (tc > 0) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < rows * tc; e += PREP_ROWS) {
+                const int rr = e / tc, tt = e % tc;
+                tile[rr * (PREP_TCHUNK + 1) + tt] = x[(size_t)(r0 + rr) * d + t0 + tt];
+            }
+            __syncthreads();
+        }
+        const int tend = min(PREP_TCHUNK, dp - t0);
+        if (r < np) {
+            for (int tt = 0; tt < tend; ++tt) {
+                float v = 0.0f;
+                if (r < n && t0 + tt < d) v = (float)((double)tile[threadIdx.x * (PREP_TCHUNK + 1) + tt] * inv);
+                xsT[(size_t)(t0 + tt) * np + r] = v;
+            }
+        }
+    }
+}
+
+// Rows of the padded range [n, np) in a block that has no real row still need zero columns.
+__global__ void k_zero_pad_cols(float* __restrict__ xsT, int n, int np, int dp) {
+    const int pad = np - n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < pad * dp; e += gridDim.x * blockDim.x) {
+        const int t = e / pad, c = n + e % pad;
+        xsT[(size_t)t * np + c] = 0.0f;
+    }
+}
+
+// lib.rs:94-102 / crates/costal-core/src/lib.rs:34-47: f32 row norms, sequential f32 sum.
+__global__ void k_row_l2_norms_f32(const float* __restrict__ x, int n, int d, float* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float s = 0.0f;
+    for (int t = 0; t < d; ++t) {
+        const float v = x[(size_t)r * d + t];
+        s = __fadd_rn(s, __fmul_rn(v, v));
+    }
+    out[r] = sqrtf(s);
+}
+
+// =================================================================================================
+// k_coarse_fp32: FP32 tiles fused with per-query top-cap selection
+// =================================================================================================
+
+namespace plain {
+
+constexpr int BM = 128;  // query rows per CTA
+constexpr int BN = 128;  // columns per tile
+constexpr int NT = 256;  // threads: 16 × 16, each an 8 × 8 register tile
+constexpr int BUF = 16;  // pending admissions per query per tile before the overflow path
+
+// (score desc, index asc) on f32 coarse scores: the heap order of knn.rs:798-801, reversed.
+__device__ __forceinline__ bool better(float sa, uint32_t ia, float sb, uint32_t ib) {
+    return sa > sb || (sa == sb && ia < ib);
+}
+
+// Insert (sv, cv) into the warp-distributed sorted list (position p = s·32 + lane), keeping the
+// best `cap`. `len` is warp-uniform.
+template <int SLOTS>
+__device__ __forceinline__ void list_insert(float (&ls)[SLOTS], uint32_t (&li)[SLOTS], int& len, int cap,
+                                            float sv, uint32_t cv, int lane) {
+    if (len == cap) {
+        const float ws = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
+        const uint32_t wi = __shfl_sync(COSTAL_FULL_MASK, li[(cap - 1) >> 5], (cap - 1) & 31);
+        if (!better(sv, cv, ws, wi)) return;
+    }
+    int pos = 0;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        const int p = s * 32 + lane;
+        const bool b = p < len && better(ls[s], li[s], sv, cv);
+        pos += __popc(__ballot_sync(COSTAL_FULL_MASK, b));
+    }
+    float ns[SLOTS];
+    uint32_t ni[SLOTS];
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        float up_s = __shfl_up_sync(COSTAL_FULL_MASK, ls[s], 1);
+        uint32_t up_i = __shfl_up_sync(COSTAL_FULL_MASK, li[s], 1);
+        if (s > 0) {
+            const float cs = __shfl_sync(COSTAL_FULL_MASK, ls[s > 0 ? s - 1 : 0], 31);
+            const uint32_t ci = __shfl_sync(COSTAL_FULL_MASK, li[s > 0 ? s - 1 : 0], 31);
+            if (lane == 0) {
+                up_s = cs;
+                up_i = ci;
+            }
+        }
+        const int p = s * 32 + lane;
+        ns[s] = p > pos ? up_s : (p == pos ? sv : ls[s]);
+        ni[s] = p > pos ? up_i : (p == pos ? cv : li[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        ls[s] = ns[s];
+        li[s] = ni[s];
+    }
+    len = len + 1 < cap ? len + 1 : cap;
+}
+
+template <int SLOTS>
+__global__ void __launch_bounds__(NT, 1)
+    k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp, int cap, int lstride,
+                  const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount,
+                  uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
+    constexpr int LCAP = 32 * SLOTS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* A_s = reinterpret_cast<float*>(smem_raw);           // [dp][BM]
+    float* B_s = A_s + (size_t)dp * BM;                         // [2][dp][BN]
+    float* L_s = B_s + (size_t)2 * dp * BN;                     // [BM][LCAP]
+    uint32_t* L_i = reinterpret_cast<uint32_t*>(L_s + BM * LCAP);
+    float* buf_s = reinterpret_cast<float*>(L_i + BM * LCAP);  // [BM][BUF]
+    uint32_t* buf_i = reinterpret_cast<uint32_t*>(buf_s + BM * BUF);
+    int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);      // [BM]
+    int* len_s = cnt_s + BM;                                    // [BM]
+    float* tau_s = reinterpret_cast<float*>(len_s + BM);        // [BM]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    // Query rows: the block's 128 consecutive rows, or 128 entries of a device-side row list (the
+    // rows a certificate sent back for an FP32 re-run).
+    const int q0 = blockIdx.x * BM;
+    const int nq = qlist ? min(BM, (int)*qcount - q0) : BM;
+    if (nq <= 0) return;
+    auto row_of = [&](int qi) -> int { return qlist ? (qi < nq ? (int)qlist[q0 + qi] : -1) : q0 + qi; };
+    const int ntiles = np / BN;
+
+    auto load_tile = [&](float* dst, int c0) {
+        for (int ch = tid; ch < dp * (BN / 4); ch += NT) {
+            const int t = ch / (BN / 4), c4 = ch % (BN / 4);
+            cp_async16(dst + t * BN + c4 * 4, xsT + (size_t)t * np + c0 + c4 * 4);
+        }
+    };
+    if (qlist) {
+        for (int e = tid; e < dp * BM; e += NT) {
+            const int t = e / BM, qi = e % BM;
+            A_s[t * BM + qi] = qi < nq ? xsT[(size_t)t * np + qlist[q0 + qi]] : 0.0f;
+        }
+    } else {
+        load_tile(A_s, q0);
+    }
+    load_tile(B_s, 0);
+    cp_async_commit();
+    if (ntiles > 1) load_tile(B_s + (size_t)dp * BN, BN);
+    cp_async_commit();
+    for (int q = tid; q < BM; q += NT) {
+        cnt_s[q] = 0;
+        len_s[q] = 0;
+        tau_s[q] = -CUDART_INF_F;
+    }
+    // Unfilled list slots read back as column 0 with score −∞ (only possible when the input holds
+    // NaN, which the host reports as an error; every index stays in range either way).
+    for (int e = tid; e < BM * LCAP; e += NT) {
+        L_s[e] = -CUDART_INF_F;
+        L_i[e] = 0u;
+    }
+
+    // Query row of register i, column of register j (two 4-wide halves 64 apart: conflict-free
+    // float4 shared-memory reads).
+    auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
+    auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
+
+    for (int tile = 0; tile < ntiles; ++tile) {
+        cp_async_wait<1>();
+        __syncthreads();
+        const float* Bst = B_s + (size_t)(tile & 1) * dp * BN;
+        const int c0 = tile * BN;
+
+        float acc[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+#pragma unroll 4
+        for (int t = 0; t < dp; ++t) {
+            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
+            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
+            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+
+        // Admission: strictly above the query's threshold at the start of the tile. Every column
+        // of an earlier tile has a smaller index than any column here, so this is the reference's
+        // strict `v > th` test (knn.rs:774-780) and keeps exactly the top-cap by (score, index).
+        float th[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) th[i] = tau_s[qi_of(i)];
+        bool hit = false;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) hit |= acc[i][j] > th[i];
+        if (hit) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (acc[i][j] > th[i]) {
+                        const int qi = qi_of(i), col = c0 + cj_of(j);
+                        if (col < n && col != row_of(qi)) {
+                            const int pos = atomicAdd(&cnt_s[qi], 1);
+                            if (pos < BUF) {
+                                buf_s[qi * BUF + pos] = acc[i][j];
+                                buf_i[qi * BUF + pos] = (uint32_t)col;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        const int pending = __syncthreads_or(hit);
+
+        if (pending) {
+            // Merge: each warp owns BM/8 queries. Buffers that overflowed are discarded and the
+            // query's tile row is recomputed (same FMA order, so the same values) and inserted
+            // column by column.
+            for (int qq = 0; qq < BM / 8; ++qq) {
+                const int qi = warp * (BM / 8) + qq;
+                const int c = cnt_s[qi];
+                if (c == 0) continue;
+                const int q = row_of(qi);
+                float ls[SLOTS];
+                uint32_t li[SLOTS];
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    ls[s] = L_s[qi * LCAP + s * 32 + lane];
+                    li[s] = L_i[qi * LCAP + s * 32 + lane];
+                }
+                int len = len_s[qi];
+                if (c <= BUF) {
+                    for (int e = 0; e < c; ++e)
+                        list_insert<SLOTS>(ls, li, len, cap, buf_s[qi * BUF + e], buf_i[qi * BUF + e], lane);
+                } else {
+                    const float th0 = tau_s[qi];
+                    for (int cc = 0; cc < BN / 32; ++cc) {
+                        const int cl = cc * 32 + lane, col = c0 + cl;
+                        float sv = 0.0f;
+                        for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
+                        unsigned m = __ballot_sync(COSTAL_FULL_MASK, col < n && col != q && sv > th0);
+                        while (m) {
+                            const int src = __ffs(m) - 1;
+                            m &= m - 1;
+                            const float v = __shfl_sync(COSTAL_FULL_MASK, sv, src);
+                            list_insert<SLOTS>(ls, li, len, cap, v, (uint32_t)(c0 + cc * 32 + src), lane);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    L_s[qi * LCAP + s * 32 + lane] = ls[s];
+                    L_i[qi * LCAP + s * 32 + lane] = li[s];
+                }
+                const float worst = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
+                if (lane == 0) {
+                    len_s[qi] = len;
+                    tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
+                    cnt_s[qi] = 0;
+                }
+            }
+            __syncthreads();
+        }
+        if (tile + 2 < ntiles) load_tile(B_s + (size_t)(tile & 1) * dp * BN, (tile + 2) * BN);
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int e = tid; e < BM * cap; e += NT) {
+        const int qi = e / cap, p = e % cap, q = row_of(qi);
+        if (q >= 0 && q < n) {
+            cand_idx[(size_t)q * lstride + p] = L_i[qi * LCAP + p];
+            cand_score[(size_t)q * lstride + p] = L_s[qi * LCAP + p];
+        }
+    }
+    for (int qi = tid; qi < BM; qi += NT) {
+        const int q = row_of(qi);
+        if (q >= 0 && q < n) tau_out[q] = tau_s[qi];
+    }
+}
+
+size_t coarse_smem_bytes(int dp, int slots) {
+    const size_t lcap = 32 * (size_t)slots;
+    return (size_t)dp * BM * 4 + 2ull * dp * BN * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 + BM * 4 * 3;
+}
+
+}  // namespace plain
+
+// =================================================================================================
+// k_rescore: f64 rescoring, sort, certificate, fused Tanimoto weight
+// =================================================================================================
+
+// Bitonic sort of a warp-distributed array (position p = s·32 + lane) into (score desc, idx asc).
+template <int SLOTS>
+__device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOTS], uint32_t (&id)[SLOTS],
+                                          int lane) {
+    constexpr int N = 32 * SLOTS;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+                const int ss = stride >> 5;
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    const int t = s ^ ss;
+                    if (t > s) {
+                        const bool asc = ((s * 32 + lane) & size) == 0;
+                        const bool sw = asc ? before64(sc[t], id[t], sc[s], id[s]) : before64(sc[s], id[s], sc[t], id[t]);
+                        if (sw) {
+                            double a = sc[s]; sc[s] = sc[t]; sc[t] = a;
+                            double b = cs[s]; cs[s] = cs[t]; cs[t] = b;
+                            uint32_t c = id[s]; id[s] = id[t]; id[t] = c;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    const double osc = __shfl_xor_sync(COSTAL_FULL_MASK, sc[s], stride);
+                    const double ocs = __shfl_xor_sync(COSTAL_FULL_MASK, cs[s], stride);
+                    const uint32_t oid = __shfl_xor_sync(COSTAL_FULL_MASK, id[s], stride);
+                    const bool lower = (lane & stride) == 0;
+                    const bool asc = ((s * 32 + lane) & size) == 0;
+                    const bool take = (lower == asc) ? before64(osc, oid, sc[s], id[s]) : before64(sc[s], id[s], osc, oid);
+                    if (take) {
+                        sc[s] = osc;
+                        cs[s] = ocs;
+                        id[s] = oid;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int SLOTS>
+__global__ void __launch_bounds__(256)
+    k_rescore(const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
+              const uint32_t* __restrict__ cand_idx, const float* __restrict__ cand_score,
+              const float* __restrict__ tau, const double* __restrict__ norms, const double* __restrict__ row_eps,
+              double eps, int certify, int select, const uint32_t* __restrict__ rlist,
+              const unsigned* __restrict__ rcount, uint32_t* __restrict__ out_idx, double* __restrict__ out_cos,
+              double* __restrict__ out_w, uint32_t* __restrict__ fb_rows, double* __restrict__ fb_minsim,
+              unsigned* __restrict__ fb_count, unsigned long long* __restrict__ max_err_bits) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (w >= (rlist ? (int)*rcount : n)) return;
+    const int i = rlist ? (int)rlist[w] : w;
+    const double ni = norms[i];
+    const float* xi = x + (size_t)i * d;
+    double sc[SLOTS], cs[SLOTS];
+    uint32_t id[SLOTS];
+    double err = 0.0;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        const int p = s * 32 + lane;
+        if (p < cap) {
+            uint32_t j = cand_idx[(size_t)i * lstride + p];
+            if (j >= (uint32_t)n) j = 0;  // only reachable on non-finite input (reported as an error)
+            const float* xj = x + (size_t)j * d;
+            double dot = 0.0;
+            for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
+            const double nj = norms[j];
+            const double c = cos64(dot, ni, nj);
+            const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
+            err = fmax(err, fabs((double)cand_score[(size_t)i * lstride + p] - score));
+            sc[s] = score;
+            cs[s] = c;
+            id[s] = j;
+        } else {
+            sc[s] = -CUDART_INF;
+            cs[s] = 0.0;
+            id[s] = 0xffffffffu;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
+    if (lane == 0 && max_err_bits) atomicMax(max_err_bits, (unsigned long long)__double_as_longlong(err));
+    warp_sort<SLOTS>(sc, cs, id, lane);
+    const double s_k = __shfl_sync(COSTAL_FULL_MASK, sc[(k - 1) >> 5], (k - 1) & 31);
+    const double e = row_eps ? row_eps[i] : eps;
+    // knn.rs:704-714: with cap == n−1 nothing was left out; otherwise exact iff s_k > τ + ε.
+    if (certify && s_k <= __dadd_rn((double)tau[i], e)) {
+        if (lane == 0) {
+            const unsigned slot = atomicAdd(fb_count, 1u);
+            fb_rows[slot] = (uint32_t)i;
+            fb_minsim[slot] = __dsub_rn(s_k, e);
+        }
+        return;
+    }
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        const int p = s * 32 + lane;
+        if (p < k) {
+            out_idx[(size_t)i * k + p] = id[s];
+            out_cos[(size_t)i * k + p] = cs[s];
+            if (out_w) out_w[(size_t)i * k + p] = tani_from_cos(ni, norms[id[s]], cs[s]);
+        }
+    }
+}
+
+// =================================================================================================
+// k_gather: full-row regather (fallback) and brute force
+// =================================================================================================
+
+constexpr int GT = 256;
+
+struct GatherSmem {
+    double* sc;
+    double* cs;
+    uint32_t* id;
+};
+
+__device__ void block_sort(double* sc, double* cs, uint32_t* id, int cnt, int capb) {
+    for (int p = cnt + threadIdx.x; p < capb; p += GT) {
+        sc[p] = -CUDART_INF;
+        cs[p] = 0.0;
+        id[p] = 0xffffffffu;
+    }
+    __syncthreads();
+    for (int size = 2; size <= capb; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int e = threadIdx.x; e < capb / 2; e += GT) {
+                const int lo = 2 * e - (e & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const bool sw = asc ? before64(sc[hi], id[hi], sc[lo], id[lo]) : before64(sc[lo], id[lo], sc[hi], id[hi]);
+                if (sw) {
+                    double a = sc[lo]; sc[lo] = sc[hi]; sc[hi] = a;
+                    double b = cs[lo]; cs[lo] = cs[hi]; cs[hi] = b;
+                    uint32_t c = id[lo]; id[lo] = id[hi]; id[hi] = c;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One CTA per row (grid-stride over the fallback list, whose length stays on the device). Keeps a
+// shared-memory buffer of rescored candidates; when it could overflow, sorts it and keeps the best
+// k (at least k candidates always qualify: the k rescored ones that defined s_k).
+__global__ void __launch_bounds__(GT)
+    k_gather(const float* __restrict__ x, const float* __restrict__ xsT, int n, int np, int d, int dp, int k,
+             const double* __restrict__ norms, const uint32_t* __restrict__ rows, const double* __restrict__ minsim,
+             const unsigned* __restrict__ count, int all_rows, int select, int capb, uint32_t* __restrict__ out_idx,
+             double* __restrict__ out_cos, double* __restrict__ out_w) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* sc = reinterpret_cast<double*>(smem_raw);
+    double* cs = sc + capb;
+    uint32_t* id = reinterpret_cast<uint32_t*>(cs + capb);
+    float* q_s = reinterpret_cast<float*>(id + capb);  // [dp] normalised query
+    float* xi_s = q_s + dp;                             // [d] raw query
+    __shared__ int cnt;
+    const int nrows = all_rows ? n : (int)*count;
+    for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
+        const int i = all_rows ? r : (int)rows[r];
+        const double ms = all_rows ? -CUDART_INF : minsim[r];
+        for (int t = threadIdx.x; t < dp; t += GT) q_s[t] = all_rows ? 0.0f : xsT[(size_t)t * np + i];
+        for (int t = threadIdx.x; t < d; t += GT) xi_s[t] = x[(size_t)i * d + t];
+        if (threadIdx.x == 0) cnt = 0;
+        __syncthreads();
+        const double ni = norms[i];
+        for (int c0 = 0; c0 < n; c0 += GT) {
+            const int c = c0 + threadIdx.x;
+            if (c < n && c != i) {
+                bool take = true;
+                if (!all_rows) {
+                    float s = 0.0f;
+                    for (int t = 0; t < dp; ++t) s = fmaf(q_s[t], xsT[(size_t)t * np + c], s);
+                    take = (double)s >= ms;
+                }
+                if (take) {
+                    double dot = 0.0;
+                    const float* xc = x + (size_t)c * d;
+                    for (int t = 0; t < d; ++t) dot = dot64_step(dot, xi_s[t], __ldg(xc + t));
+                    const double nj = norms[c];
+                    const double cv = cos64(dot, ni, nj);
+                    const int pos = atomicAdd(&cnt, 1);
+                    sc[pos] = select == 0 ? cv : tani_from_cos(ni, nj, cv);
+                    cs[pos] = cv;
+                    id[pos] = (uint32_t)c;
+                }
+            }
+            __syncthreads();
+            if (cnt > capb - GT) {
+                block_sort(sc, cs, id, cnt, capb);
+                if (threadIdx.x == 0) cnt = k;
+                __syncthreads();
+            }
+        }
+        block_sort(sc, cs, id, cnt, capb);
+        for (int p = threadIdx.x; p < k; p += GT) {
+            out_idx[(size_t)i * k + p] = id[p];
+            out_cos[(size_t)i * k + p] = cs[p];
+            if (out_w) out_w[(size_t)i * k + p] = tani_from_cos(ni, norms[id[p]], cs[p]);
+        }
+        __syncthreads();
+    }
+}
+
+// =================================================================================================
+// launchers
+// =================================================================================================
+
+cudaError_t launch_prep(const float* x, int n, int d, int np, int dp, double* norms, float* xsT,
+                        unsigned long long* bad_row, cudaStream_t st) {
+    const int blocks = (np + PREP_ROWS - 1) / PREP_ROWS;
+    k_prep<<<blocks, PREP_ROWS, 0, st>>>(x, n, d, np, dp, norms, xsT, bad_row);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cudaStream_t st) {
+    k_row_l2_norms_f32<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out);
+    return cudaGetLastError();
+}
+
+int coarse_slots(int cap) { return cap <= 32 ? 1 : (cap <= 64 ? 2 : (cap <= 128 ? 4 : 0)); }
+
+size_t coarse_fp32_smem(int dp, int cap) { return plain::coarse_smem_bytes(dp, coarse_slots(cap)); }
+
+cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                               const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
+                               cudaStream_t st) {
+    const int slots = coarse_slots(cap);
+    const size_t smem = plain::coarse_smem_bytes(dp, slots);
+    const int blocks = np / plain::BM;
+    cudaError_t e;
+#define COSTAL_COARSE(S)                                                                                    \
+    e = cudaFuncSetAttribute(plain::k_coarse_fp32<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e;                                                                         \
+    plain::k_coarse_fp32<S><<<blocks, plain::NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, \
+                                                                    cand_score, tau);
+    if (slots == 1) {
+        COSTAL_COARSE(1)
+    } else if (slots == 2) {
+        COSTAL_COARSE(2)
+    } else {
+        COSTAL_COARSE(4)
+    }
+#undef COSTAL_COARSE
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
+                           const float* cand_score, const float* tau, const double* norms, const double* row_eps,
+                           double eps, int certify, int select, const uint32_t* rlist, const unsigned* rcount,
+                           uint32_t* out_idx, double* out_cos, double* out_w, uint32_t* fb_rows, double* fb_minsim,
+                           unsigned* fb_count, unsigned long long* max_err_bits, cudaStream_t st) {
+    const int slots = coarse_slots(cap);
+    const int blocks = (n + 7) / 8;
+#define COSTAL_RESCORE(S)                                                                                   \
+    k_rescore<S><<<blocks, 256, 0, st>>>(x, n, d, k, cap, lstride, cand_idx, cand_score, tau, norms, row_eps, \
+                                         eps, certify, select, rlist, rcount, out_idx, out_cos, out_w, fb_rows, \
+                                         fb_minsim,                                                           \
+                                         fb_count, max_err_bits);
+    if (slots == 1) {
+        COSTAL_RESCORE(1)
+    } else if (slots == 2) {
+        COSTAL_RESCORE(2)
+    } else {
+        COSTAL_RESCORE(4)
+    }
+#undef COSTAL_RESCORE
+    return cudaGetLastError();
+}
+
+int gather_capb(int k) {
+    int c = 512;
+    while (c < k + GT) c <<= 1;
+    return c;
+}
+
+size_t gather_smem(int k, int d, int dp) { return (size_t)gather_capb(k) * 20 + (size_t)(dp + d) * 4 + 16; }
+
+cudaError_t launch_gather(const float* x, const float* xsT, int n, int np, int d, int dp, int k, const double* norms,
+                          const uint32_t* rows, const double* minsim, const unsigned* count, int all_rows, int select,
+                          int grid, uint32_t* out_idx, double* out_cos, double* out_w, cudaStream_t st) {
+    const int capb = gather_capb(k);
+    const size_t smem = gather_smem(k, d, dp);
+    cudaError_t e = cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_gather<<<grid, GT, smem, st>>>(x, xsT, n, np, d, dp, k, norms, rows, minsim, count, all_rows, select, capb,
+                                     out_idx, out_cos, out_w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_pad(float* xsT, int n, int np, int dp, cudaStream_t st) {
+    if (np == n) return cudaSuccess;
+    k_zero_pad_cols<<<64, 256, 0, st>>>(xsT, n, np, dp);
+    return cudaGetLastError();
+}
+
+}  // namespace costal

@@ -1,0 +1,32 @@
+// Certified split-BF16 coarse pass on the 5th-generation tensor cores (tcgen05, TMEM accumulators).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace costal {
+namespace tc {
+
+constexpr int BLOCK_M = 128;  // query rows per CTA tile (the MMA's M; one TMEM lane per query)
+constexpr int BLOCK_N = 256;  // columns per tile (the MMA's N)
+
+struct Plan {
+    int n, d, np, kp;       // rows, features, padded rows, padded K of the split operands
+    const void* ops_a;      // [np][kp] bf16 query operand   (hi | lo | hi)
+    const void* ops_b;      // [np][kp] bf16 column operand  (hi | hi | lo)
+    const double* row_eps;  // [n] certificate bound of each query row
+    const double* col_max;  // [4] maxima over all rows of the split-residual norms
+};
+
+bool supported(int d, int cap);
+size_t workspace_bytes(int n, int d);
+// Split the normalised rows (xsT, d_pad × n_pad) into BF16 operands and per-row error norms, and
+// derive each row's certificate bound.
+cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, cudaStream_t st, Plan& plan);
+// All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
+cudaError_t launch_coarse(const Plan& plan, int cap, uint32_t* cand_idx, float* cand_score, float* tau,
+                          unsigned long long* timeout_flag, int sm_count, cudaStream_t st);
+
+}  // namespace tc
+}  // namespace costal

@@ -1,0 +1,127 @@
+/* costal_gb300 — C ABI of the GB300 (sm_103a) exact cosine kNN graph.
+ *
+ * Drop-in boundary for CosTaL 2.1.0's `costal._costal` extension (crates/costal-py/src/lib.rs). Each
+ * entry point replaces the reference function named beside it; the Python module
+ * costal_gb300/_costal.py binds them with the reference's exact signatures.
+ *
+ * Conventions:
+ *  - plain pointers and sizes only; arrays are row-major and C-contiguous;
+ *  - entry points whose name does not end in `_device` take HOST pointers and do their own
+ *    host<->device copies; `_device` entry points take DEVICE pointers and a cudaStream_t (as void*);
+ *  - every entry point returns a status (COSTAL_OK = 0) and, on failure, writes a NUL-terminated
+ *    message into `err` (at most `errlen` bytes). Nothing aborts or exits the process;
+ *  - calls are serialised on one cached per-process device context (a mutex), so they are re-entrant
+ *    from several host threads.
+ */
+#ifndef COSTAL_GB300_H
+#define COSTAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define COSTAL_OK 0
+#define COSTAL_EINVAL 2     /* invalid input: the reference raises ValueError (lib.rs:31-33) */
+#define COSTAL_ECUDA 3      /* a CUDA call failed, or no usable GB300 device */
+#define COSTAL_ENOMEM 4     /* a device allocation failed */
+#define COSTAL_ETIMEOUT 5   /* a bounded device-side wait gave up; the context stays usable */
+#define COSTAL_EUNSUPPORTED 6 /* valid input outside what the GPU kernels support (e.g. k + margin > 128) */
+
+/* Coarse-pass backends. Like the reference's `matmul` knob (crates/costal-core/src/matmul.rs:10-50)
+ * they change speed only, never the output. */
+#define COSTAL_BACKEND_FP32 0  /* plain FP32 CUDA-core tiles: the default drop-in */
+#define COSTAL_BACKEND_BF16 1  /* certified split-BF16 tcgen05 tiles, FP32 accumulate in TMEM */
+
+#define COSTAL_SELECT_COSINE 0
+#define COSTAL_SELECT_TANIMOTO 1
+
+#define COSTAL_WEIGHT_TANIMOTO 0
+#define COSTAL_WEIGHT_COSINE 1
+#define COSTAL_WEIGHT_JACCARD 2
+
+/* Options of an exact kNN call: KnnParams (crates/costal-core/src/knn.rs:27-60) plus the backend. */
+typedef struct costal_knn_opts {
+    uint32_t margin;       /* over-selection m; UINT32_MAX = the reference default m = k (knn.rs:52) */
+    uint32_t select;       /* COSTAL_SELECT_*; knn.rs:64-69 */
+    uint32_t backend;      /* COSTAL_BACKEND_* */
+    uint32_t row_block;    /* accepted for compatibility (knn.rs:35-37); speed-only, 0 = derive */
+    uint32_t col_block;    /* idem */
+    int32_t sort_by_norm;  /* idem (knn.rs:41): output-independent */
+    int32_t prune;         /* idem (knn.rs:44): output-independent */
+    int32_t learned_prune; /* 1 = use the trained block-pruning model if one is loaded (bf16 backend) */
+} costal_knn_opts;
+
+/* KnnStats (knn.rs:346-357) plus the GPU path's own counters. */
+typedef struct costal_knn_stats {
+    uint64_t fallback_rows;    /* rows that took the full-row regather (knn.rs:704-714) */
+    uint64_t row_block;        /* query rows per CTA tile */
+    uint64_t col_block;        /* columns per tile */
+    uint64_t blocks_skipped;   /* (row block, column block) tiles skipped by pruning */
+    uint64_t blocks_total;     /* row blocks x column blocks */
+    uint64_t margin;           /* the m in effect */
+    uint64_t recomputed_rows;  /* bf16 backend: rows whose certificate failed, redone in FP32 */
+    uint64_t pruned_fallback_rows; /* learned pruning: rows whose skip was not certified, rescanned */
+    double max_coarse_err;     /* max |coarse score - f64 rescored score| over all kept candidates */
+    double ms_prep, ms_coarse, ms_rescore, ms_fallback, ms_total; /* CUDA-event times of the stages */
+} costal_knn_stats;
+
+/* ---- module surface (crates/costal-py/src/lib.rs:80-102, 430-446) ---------------------------- */
+const char* costal_version(void);   /* replaces env!("CARGO_PKG_VERSION") of lib.rs:450 */
+int costal_device_ok(char* err, size_t errlen);  /* 0 when a usable sm_103 device is present */
+/* lib.rs:94-102 (costal_core::row_l2_norms, crates/costal-core/src/lib.rs:34-47): f32 row norms. */
+int costal_row_l2_norms(const float* x, uint64_t n, uint32_t d, float* out, char* err, size_t errlen);
+
+/* ---- the hot path ------------------------------------------------------------------------------ */
+/* lib.rs:114-167 `_knn_exact` -> knn.rs:365 knn_exact_with_stats. Host buffers: x n*d f32;
+ * idx n*k, cos n*k, norms n. */
+int costal_knn_exact(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                     uint32_t* idx, double* cos, double* norms, costal_knn_stats* stats, char* err,
+                     size_t errlen);
+/* The same on device buffers, on `stream` (a cudaStream_t; NULL = the library's stream). */
+int costal_knn_exact_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                            uint32_t* d_idx, double* d_cos, double* d_norms, costal_knn_stats* stats,
+                            void* stream, char* err, size_t errlen);
+/* lib.rs:172-191 `_knn_bruteforce` -> knn.rs:884 knn_bruteforce_select: every candidate in f64. */
+int costal_knn_bruteforce(const float* x, uint64_t n, uint32_t d, uint32_t k, uint32_t select, uint32_t* idx,
+                          double* cos, double* norms, char* err, size_t errlen);
+/* lib.rs:195-214 `_reweight` -> weight.rs:41 reweight. idx values are checked to be in [0, n). */
+int costal_reweight(uint64_t n, uint32_t k, const int32_t* idx, const double* cos, const double* norms,
+                    uint32_t weight, double* out, char* err, size_t errlen);
+/* lib.rs:219-239 `_fuzzy_union` -> graph.rs:24 fuzzy_union. rows/cols/w hold up to n*k edges;
+ * *m receives the edge count. */
+int costal_fuzzy_union(uint64_t n, uint32_t k, const int32_t* idx, const double* w, int32_t* rows,
+                       int32_t* cols, double* w_out, uint64_t* m, char* err, size_t errlen);
+/* The fused device pipeline of _api.py:460-462 (knn -> reweight -> _fuzzy_union): X goes up once,
+ * the kNN stays on the device, and only the edge list (and the kNN, if idx/cos/norms are not
+ * NULL) comes back. rows/cols/w hold up to n*k edges. */
+int costal_build_graph(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                       uint32_t weight, int32_t* rows, int32_t* cols, double* w, uint64_t* m, uint32_t* idx,
+                       double* cos, double* norms, costal_knn_stats* stats, char* err, size_t errlen);
+/* The same from device-resident X, with device outputs (capacity n*k edges); *m is written on the host. */
+int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                              uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m,
+                              costal_knn_stats* stats, void* stream, char* err, size_t errlen);
+
+/* ---- the host consumer: Leiden (leiden="fast"), crates/costal-core/src/leiden.rs ------------- */
+/* lib.rs:275-306 `_leiden` (from_coo = 0, objective = 0) and lib.rs:356-412 `_leiden_coo`
+ * (from_coo = 1). objective: 0 modularity, 1 CPM. initial may be NULL. quality may be NULL. */
+int costal_leiden(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
+                  int objective, int from_coo, double resolution, double beta, int32_t n_iterations,
+                  uint64_t seed, const uint32_t* initial, uint32_t* membership, uint64_t* n_clusters,
+                  uint64_t* iterations, int* converged, double* quality, char* err, size_t errlen);
+/* lib.rs:311-350 `_leiden_many`: out is (n_resolutions * n_seeds) x n, resolutions outer. */
+int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
+                       const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
+                       double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen);
+/* lib.rs:416-428 `_modularity`. */
+int costal_modularity(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
+                      const uint32_t* membership, double resolution, double* q, char* err, size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COSTAL_GB300_H */

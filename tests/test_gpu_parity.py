@@ -1,0 +1,285 @@
+"""GPU parity: the CUDA path (through the C ABI, via costal_gb300._costal) against the CPU oracle.
+
+Integer and index outputs must be bit-identical, and so must the f64 cosines, norms and weights
+(the reference's order of operations is restated on the device). Restates the reference's
+tests/test_knn.py and knn.rs unit tests, plus full-size checks on the benchmark workloads through
+row samples (the oracle answers a sample of query rows against all n columns).
+"""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_PIPELINE, Lcg, clustered, digest, lcg_clustered, pipeline_input
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b):
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(np.asarray(u), np.asarray(v))
+
+
+def as_oracle(res):
+    idx, cos, norms = res
+    return idx.view(np.uint32), cos, norms
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_exact_matches_bruteforce_bitwise(ext, oracle, seed):
+    # test_knn.py:36-43
+    x = clustered(3000, 32, seed)
+    got, stats = ext._knn_exact(x, 10)
+    same(as_oracle(got), oracle.knn_bruteforce(x, 10))
+    same(as_oracle(ext._knn_bruteforce(x, 10)), oracle.knn_bruteforce(x, 10))
+    assert stats["fallback_rows"] == 0
+
+
+def test_matches_independent_numpy_oracle(ext):
+    # test_knn.py:46-61
+    x = clustered(1500, 20, 2)
+    idx, cos, _ = ext._knn_exact(x, 12)[0]
+    x64 = x.astype(np.float64)
+    xn = x64 / np.linalg.norm(x64, axis=1, keepdims=True)
+    sim = xn @ xn.T
+    np.fill_diagonal(sim, -np.inf)
+    order = np.argsort(-sim, axis=1, kind="stable")[:, :13]
+    want = np.take_along_axis(sim, order, axis=1)
+    np.testing.assert_allclose(cos, want[:, :12], rtol=0, atol=1e-12)
+    clear = (want[:, 11] - want[:, 12]) > 1e-9
+    assert clear.mean() > 0.99
+    for i in np.flatnonzero(clear):
+        assert set(idx[i]) == set(order[i, :12])
+
+
+def test_output_independent_of_knobs_and_backend(ext, oracle):
+    # test_knn.py:64-75: blocks, backend, layout and threads never change the output
+    x = clustered(1200, 17, 3)
+    want = oracle.knn_bruteforce(x, 7)
+    for backend in ("gemm", ext.default_matmul(), "bf16"):
+        for rb, cb in [(1, 7), (16, 128), (200, 5000)]:
+            for sort in (False, True):
+                got, _ = ext._knn_exact(x, 7, row_block=rb, col_block=cb, matmul=backend, sort_by_norm=sort,
+                                        n_threads=3)
+                same(as_oracle(got), want)
+
+
+def test_ties_break_by_original_index(ext, oracle):
+    # test_knn.py:78-84
+    rng = np.random.default_rng(4)
+    protos = rng.normal(size=(10, 5)).astype(np.float32)
+    x = np.ascontiguousarray(np.tile(protos, (30, 1)))
+    idx, cos, norms = ext._knn_exact(x, 10)[0]
+    same(as_oracle((idx, cos, norms)), oracle.knn_bruteforce(x, 10))
+    np.testing.assert_array_equal(idx[0], np.arange(10, 101, 10))
+
+
+def test_tie_heavy_integer_data_stays_exact(ext, oracle):
+    # test_knn.py:87-94: massive exact ties must take the regather fallback
+    rng = np.random.default_rng(5)
+    x = np.floor(rng.uniform(0, 3, size=(500, 6))).astype(np.float32)
+    x[[0, 99, 499]] = 0.0
+    got, stats = ext._knn_exact(x, 12)
+    same(as_oracle(got), oracle.knn_bruteforce(x, 12))
+    assert stats["fallback_rows"] > 0
+
+
+def test_lcg_known_answers(ext, oracle):
+    # knn.rs:1001-1044 on the reference's own generator
+    g = Lcg(3)
+    protos = np.array([np.float32(g.next_f32() - np.float32(0.3)) for _ in range(50)], np.float32).reshape(10, 5)
+    x = np.ascontiguousarray(protos[np.arange(300) % 10])
+    idx = ext._knn_exact(x, 10)[0][0]
+    assert list(idx[0]) == [10, 20, 30, 40, 50, 60, 70, 80, 90, 100]
+    g = Lcg(4)
+    x = np.array([np.floor(g.next_f32() * np.float32(3.0)) for _ in range(2400)], np.float32).reshape(400, 6)
+    x[[0, 57, 399]] = 0.0
+    got = ext._knn_exact(x, 12)[0]
+    same(as_oracle(got), oracle.knn_bruteforce(x, 12))
+    assert (got[1][0] == 0.0).all()
+    x = lcg_clustered(25, 4, 5)
+    for k in (1, 23, 24):
+        same(as_oracle(ext._knn_exact(x, k)[0]), oracle.knn_bruteforce(x, k))
+
+
+@pytest.mark.parametrize("n,d,k,margin", [(1001, 1, 5, None), (777, 5, 1, 0), (1500, 15, 10, 8), (1300, 17, 7, None),
+                                          (900, 33, 30, None), (640, 64, 12, 3), (2000, 40, 10, 118), (129, 3, 20, 0)])
+def test_shapes_and_margins(ext, oracle, n, d, k, margin):
+    rng = np.random.default_rng(n * 31 + d)
+    means = rng.normal(0, 2, size=(7, d))
+    x = np.arcsinh((means[rng.integers(0, 7, n)] + rng.normal(0, 0.6, size=(n, d))) / 5.0).astype(np.float32)
+    got, st = ext._knn_exact(x, k, margin=margin)
+    want, ost = oracle.knn_exact(x, k, margin=margin)
+    same(as_oracle(got), want)
+    same(as_oracle(got), oracle.knn_bruteforce(x, k))
+
+
+def test_tanimoto_selection_matches_bruteforce(ext, oracle):
+    # test_knn.py:118-126
+    x = clustered(1500, 12, 14)
+    x *= np.random.default_rng(114).uniform(0.5, 3.0, size=(1500, 1)).astype(np.float32)
+    x = np.ascontiguousarray(x)
+    got, stats = ext._knn_exact(x, 10, select="tanimoto")
+    assert stats["select"] == "tanimoto"
+    same(as_oracle(got), oracle.knn_bruteforce(x, 10, select="tanimoto"))
+    same(as_oracle(ext._knn_bruteforce(x, 10, select="tanimoto")), oracle.knn_bruteforce(x, 10, select="tanimoto"))
+    assert not np.array_equal(got[0], ext._knn_exact(x, 10)[0][0])
+
+
+@pytest.mark.parametrize("weight", ["tanimoto", "cosine", "jaccard"])
+def test_reweight_bitwise(ext, oracle, weight):
+    x = clustered(2000, 12, 8)
+    idx, cos, norms = ext._knn_exact(x, 10)[0]
+    np.testing.assert_array_equal(ext._reweight(idx, cos, norms, weight),
+                                  oracle.reweight(idx.view(np.uint32), cos, norms, weight))
+
+
+def test_reweight_rejects_out_of_range(ext):
+    idx = np.array([[1, 2], [0, 5], [0, 1]], np.int32)
+    with pytest.raises(ValueError, match="neighbor index 5 out of range"):
+        ext._reweight(idx, np.zeros((3, 2)), np.ones(3), "tanimoto")
+
+
+def test_fuzzy_union_bitwise(ext, oracle):
+    x = clustered(3000, 16, 10)
+    idx, cos, norms = ext._knn_exact(x, 10)[0]
+    w = ext._reweight(idx, cos, norms, "tanimoto")
+    got = ext._fuzzy_union(idx, w)
+    want = oracle.fuzzy_union(idx.view(np.uint32), w)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b.astype(a.dtype) if a.dtype != np.float64 else b)
+
+
+def test_fuzzy_union_edge_cases(ext, oracle):
+    # self-loops, exact zeros, one-sided and two-sided pairs, a hub with a large in-degree
+    rng = np.random.default_rng(0)
+    n, k = 5000, 6
+    idx = rng.integers(0, n, size=(n, k)).astype(np.int32)
+    idx[:, 0] = np.arange(n)          # self-loops are dropped
+    idx[::3, 1] = 7                   # node 7: in-degree > 1600 (the large-bucket sort path)
+    for i in range(n):                # de-duplicate within rows (kNN rows hold distinct neighbours)
+        row = list(dict.fromkeys(idx[i].tolist()))
+        while len(row) < k:
+            c = int(rng.integers(0, n))
+            if c not in row:
+                row.append(c)
+        idx[i] = row
+    w = rng.uniform(-0.3, 1.0, size=(n, k))
+    w[rng.random((n, k)) < 0.05] = 0.0
+    got = ext._fuzzy_union(idx, w)
+    want = oracle.fuzzy_union(idx.view(np.uint32), w)
+    np.testing.assert_array_equal(got[0], want[0].astype(np.int32))
+    np.testing.assert_array_equal(got[1], want[1].astype(np.int32))
+    np.testing.assert_array_equal(got[2], want[2])
+
+
+@pytest.mark.parametrize("weight", ["tanimoto", "cosine", "jaccard"])
+def test_fused_build_graph_equals_separate_calls(ext, weight):
+    x = clustered(2500, 20, 11)
+    (rows, cols, w), knn, st = ext._build_graph(x, 10, weight=weight, return_knn=True)
+    idx, cos, norms = ext._knn_exact(x, 10)[0]
+    same(knn, (idx, cos, norms))
+    want = ext._fuzzy_union(idx, ext._reweight(idx, cos, norms, weight))
+    same((rows, cols, w), want)
+
+
+def test_golden_pipeline_digest_on_gpu(ext):
+    # test_leiden_native.py:129-135 with the graph built on the GPU and Leiden on the host
+    x = pipeline_input()
+    (idx, cos, norms), _ = ext._knn_exact(x, 10, select="cosine")
+    w = ext._reweight(idx, cos, norms, "tanimoto")
+    rows, cols, ew = ext._fuzzy_union(idx, w)
+    m = ext._leiden(len(x), rows, cols, ew, resolution=0.8, n_iterations=2, seed=3)[0]
+    assert digest(m.astype(np.int64)) == GOLDEN_PIPELINE
+    rows2, cols2, ew2 = ext._build_graph(x, 10)
+    m2 = ext._leiden(len(x), rows2, cols2, ew2, resolution=0.8, n_iterations=2, seed=3)[0]
+    assert digest(m2.astype(np.int64)) == GOLDEN_PIPELINE
+
+
+def test_golden_fixtures(ext):
+    from pathlib import Path
+
+    for f in sorted((Path(__file__).parent / "golden").glob("*.npz")):
+        z = np.load(f)
+        (idx, cos, norms), st = ext._knn_exact(z["x"], int(z["k"]), margin=int(z["margin"]))
+        np.testing.assert_array_equal(idx, z["idx"].view(np.int32))
+        np.testing.assert_array_equal(cos, z["cos"])
+        np.testing.assert_array_equal(norms, z["norms"])
+        w = ext._reweight(idx, cos, norms, "tanimoto")
+        np.testing.assert_array_equal(w, z["w"])
+        r, c, v = ext._fuzzy_union(idx, w)
+        np.testing.assert_array_equal(r, z["rows"].view(np.int32))
+        np.testing.assert_array_equal(c, z["cols"].view(np.int32))
+        np.testing.assert_array_equal(v, z["ew"])
+
+
+def test_input_validation(ext):
+    # test_knn.py:151-171 (through the module surface)
+    x = clustered(50, 4, 7)
+    with pytest.raises(ValueError, match="invalid k=50"):
+        ext._knn_exact(x, 50)
+    with pytest.raises(ValueError, match="invalid k=0"):
+        ext._knn_exact(x, 0)
+    bad = x.copy()
+    bad[3, 1] = np.nan
+    with pytest.raises(ValueError, match="row 3 contains NaN"):
+        ext._knn_exact(bad, 5)
+    bad[3, 1] = np.inf
+    with pytest.raises(ValueError, match="NaN or inf"):
+        ext._knn_bruteforce(bad, 5)
+    # the context stays usable after an input error
+    same(as_oracle(ext._knn_exact(x, 5)[0]), as_oracle(ext._knn_bruteforce(x, 5)))
+
+
+def test_row_l2_norms(ext):
+    # test_smoke.py:18-26
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((257, 33), dtype=np.float32)
+    got = ext.row_l2_norms(x)
+    assert got.dtype == np.float32 and got.shape == (257,)
+    np.testing.assert_allclose(got, np.linalg.norm(x, axis=1), rtol=1e-5, atol=1e-5)
+
+
+# ---- the benchmark workloads -------------------------------------------------------------------
+
+def test_mixture_20k_full_parity_and_labels(ext, oracle):
+    """Config 1 (20,000 × 32, k = 10): the whole kNN, weights, graph and Leiden labels."""
+    from costal_gb300 import workloads as W
+
+    x, wl = W.make("mixture_20k")
+    (idx, cos, norms), st = ext._knn_exact(x, wl.k)
+    want, _ = oracle.knn_exact(x, wl.k)
+    same(as_oracle((idx, cos, norms)), want)
+    rows, cols, w = ext._build_graph(x, wl.k)
+    ow = oracle.reweight(want[0], want[1], want[2], "tanimoto")
+    orows, ocols, oew = oracle.fuzzy_union(want[0], ow)
+    np.testing.assert_array_equal(rows, orows.view(np.int32))
+    np.testing.assert_array_equal(cols, ocols.view(np.int32))
+    np.testing.assert_array_equal(w, oew)
+    m = ext._leiden(len(x), rows, cols, w, resolution=0.8, n_iterations=2, seed=0)[0]
+    mo = ext._leiden(len(x), orows.view(np.int32), ocols.view(np.int32), oew, resolution=0.8, n_iterations=2, seed=0)[0]
+    np.testing.assert_array_equal(m, mo)
+
+
+@pytest.mark.parametrize("name,rows", [("rare_400k", 3000), ("dense_dup_160k", 2000), ("zipf_2m", 600)])
+@pytest.mark.parametrize("backend", ["fp32", "bf16"])
+def test_full_size_row_sample_parity(ext, oracle, name, rows, backend):
+    """Full-size inputs: the GPU answer for a seeded sample of query rows equals the oracle's
+    answer for those rows against all n columns (bit-exact), and every row satisfies the output
+    invariants (no self, distinct neighbours, sorted by (cos desc, index asc))."""
+    from costal_gb300 import workloads as W
+
+    x, wl = W.make(name)
+    n = len(x)
+    (idx, cos, norms), st = ext._knn_exact(x, wl.k, margin=wl.margin, matmul=backend)
+    q0 = int(np.random.default_rng(wl.seed).integers(0, n - rows))
+    (oidx, ocos, onorms), _ = oracle.knn_rows(x, wl.k, q0, q0 + rows, margin=wl.margin)
+    np.testing.assert_array_equal(norms, onorms)
+    np.testing.assert_array_equal(idx[q0:q0 + rows].view(np.uint32), oidx)
+    np.testing.assert_array_equal(cos[q0:q0 + rows], ocos)
+    assert not (idx == np.arange(n)[:, None]).any()
+    d = np.diff(cos, axis=1)
+    assert (d <= 0).all()
+    tie = d == 0
+    assert (np.diff(idx, axis=1)[tie] > 0).all()
+    s = np.sort(idx, axis=1)
+    assert (np.diff(s, axis=1) > 0).all()
