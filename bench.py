@@ -162,6 +162,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rare_400k")
+    ap.add_argument("--n", type=int, default=None, help="a smaller n from the same generator (profiling)")
     ap.add_argument("--backend", default="fp32", choices=["fp32", "bf16"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -171,7 +172,11 @@ def main():
 
     from costal_gb300 import workloads as W
 
-    x, wl = W.make(args.workload)
+    x, wl = W.make(args.workload, n=args.n)
+    if args.n is not None:
+        import dataclasses
+
+        wl = dataclasses.replace(wl, n=len(x))
     if args.impl == "reference":
         return run_reference(args, wl, x)
 
