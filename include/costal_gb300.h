@@ -105,6 +105,15 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
                               uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m,
                               costal_knn_stats* stats, void* stream, char* err, size_t errlen);
 
+/* Jaccard weights (the computation of costal_reweight with COSTAL_WEIGHT_JACCARD) on DEVICE buffers,
+ * for callers that may not allocate device memory: it has no counterpart in the reference. Its scratch is
+ * a fixed 16 MiB array compiled into the library (reserved on every GPU that loads it, until the process
+ * exits), so n*k is limited to 4,194,304 neighbour entries; larger inputs return COSTAL_EINVAL before any
+ * device work. The first call on a device looks up that array's address (make it before any stream
+ * capture). All calls share the array: calls that overlap on the GPU race and must be serialised. */
+int costal_reweight_jaccard_device_noalloc(const int32_t* d_idx, uint64_t n, uint32_t k, double* d_out, void* stream,
+                                           char* err, size_t errlen);
+
 /* ---- the host consumer: Leiden (leiden="fast"), crates/costal-core/src/leiden.rs ------------- */
 /* lib.rs:275-306 `_leiden` (from_coo = 0, objective = 0) and lib.rs:356-412 `_leiden_coo`
  * (from_coo = 1). objective: 0 modularity, 1 CPM. initial may be NULL. quality may be NULL. */
