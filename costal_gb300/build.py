@@ -72,7 +72,7 @@ def build_library(force: bool = False, verbose: bool = False, ptxas_info: bool =
     jobs = []
     for src in cu:
         obj = BUILD / (src.stem + ".cu.o")
-        flags = NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else [])
+        flags = NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + os.environ.get("COSTAL_NVCC_EXTRA", "").split()
         jobs.append([nvcc, *flags, "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD / (src.stem + ".cpp.o")

@@ -144,7 +144,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
              double* d_cos, double* d_norms, double* d_w, costal_knn_stats* st, cudaStream_t s) {
     const uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
     const int cap = (int)std::min<uint64_t>((uint64_t)k + margin, (uint64_t)n - 1);
-    const int dp = round_up(std::max(d, 1), 4);
+    const int dp = coarse_dpad(d);
     const int np = round_up(n, 128);
     if (coarse_slots(cap) == 0)
         throw Fail{COSTAL_EUNSUPPORTED, "k + margin = " + std::to_string(k + margin) +
@@ -359,7 +359,7 @@ int costal_knn_bruteforce(const float* x, uint64_t n, uint32_t d, uint32_t k, ui
     return guarded(err, errlen, [&](Context& c) {
         check_knn_args(n, d, k);
         cudaStream_t s = c.stream;
-        const int dp = round_up(std::max((int)d, 1), 4), np = round_up((int)n, 128);
+        const int dp = coarse_dpad((int)d), np = round_up((int)n, 128);
         CK(ensure(c.x, n * d * 4ull));
         CK(ensure(c.out_idx, n * k * 4ull));
         CK(ensure(c.out_cos, n * k * 8ull));

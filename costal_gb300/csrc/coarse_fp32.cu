@@ -1,0 +1,354 @@
+// The FP32 coarse pass: every (query block × column tile) dot product on the CUDA cores, fused with
+// the per-query top-cap selection (crates/costal-core/src/knn.rs:603-660 tiles, :758-787 the
+// threshold scan, :791-875 the per-row heaps).
+//
+// Layout: 256 threads per CTA own 128 query rows; each thread holds an 8 × 8 register tile (queries
+// ty·4+i and 64+ty·4+i, columns tx·4+j and 64+tx·4+j), so all 128 columns of a query's tile row are
+// computed inside ONE warp. The normalised rows are read transposed (xsT, d_pad × n_pad) so that a
+// tile is d_pad contiguous 512-byte rows, staged by cp.async in a 3-stage shared-memory ring: one
+// block barrier per tile, and the top-cap merges are warp-local (no block barrier).
+//
+// Selection: each query keeps its best `cap` columns by (score desc, index asc) in shared memory,
+// with τ = the worst kept score (−∞ until full). A column is admitted when its score is strictly
+// above the τ of the tile start; since every earlier tile holds smaller column indices, that is the
+// reference's strict `v > th` test and the kept set is exactly the top-cap (knn.rs:774-780).
+// Admissions go to a 16-entry buffer per query; a query whose buffer overflows (early tiles) has its
+// tile row recomputed by its warp in the same FMA order and inserted column by column.
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace costal {
+namespace plain {
+
+constexpr int BM = 128;
+constexpr int BN = 128;
+constexpr int NT = 256;
+constexpr int BUF = 16;
+constexpr int STAGES = 3;
+
+#ifndef COSTAL_FP32_PAIRED
+#define COSTAL_FP32_PAIRED 1
+#endif
+
+__device__ __forceinline__ unsigned long long pack2(float x, float y) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long r, float& x, float& y) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ bool better(float sa, uint32_t ia, float sb, uint32_t ib) {
+    return sa > sb || (sa == sb && ia < ib);
+}
+
+// Insert (sv, cv) into the warp-distributed sorted list (position p = s·32 + lane), keeping the best
+// `cap`. `len` is warp-uniform.
+template <int SLOTS>
+__device__ __forceinline__ void list_insert(float (&ls)[SLOTS], uint32_t (&li)[SLOTS], int& len, int cap, float sv,
+                                            uint32_t cv, int lane) {
+    if (len == cap) {
+        const float ws = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
+        const uint32_t wi = __shfl_sync(COSTAL_FULL_MASK, li[(cap - 1) >> 5], (cap - 1) & 31);
+        if (!better(sv, cv, ws, wi)) return;
+    }
+    int pos = 0;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        const int p = s * 32 + lane;
+        pos += __popc(__ballot_sync(COSTAL_FULL_MASK, p < len && better(ls[s], li[s], sv, cv)));
+    }
+    float ns[SLOTS];
+    uint32_t ni[SLOTS];
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        float up_s = __shfl_up_sync(COSTAL_FULL_MASK, ls[s], 1);
+        uint32_t up_i = __shfl_up_sync(COSTAL_FULL_MASK, li[s], 1);
+        if (s > 0) {
+            const float cs = __shfl_sync(COSTAL_FULL_MASK, ls[s > 0 ? s - 1 : 0], 31);
+            const uint32_t ci = __shfl_sync(COSTAL_FULL_MASK, li[s > 0 ? s - 1 : 0], 31);
+            if (lane == 0) {
+                up_s = cs;
+                up_i = ci;
+            }
+        }
+        const int p = s * 32 + lane;
+        ns[s] = p > pos ? up_s : (p == pos ? sv : ls[s]);
+        ni[s] = p > pos ? up_i : (p == pos ? cv : li[s]);
+    }
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        ls[s] = ns[s];
+        li[s] = ni[s];
+    }
+    len = len + 1 < cap ? len + 1 : cap;
+}
+
+template <int SLOTS, int DPC>
+__global__ void __launch_bounds__(NT, 1)
+    k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp_rt, int cap, int lstride,
+                  const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount,
+                  uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
+    constexpr int LCAP = 32 * SLOTS;
+    const int dp = DPC ? DPC : dp_rt;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* A_s = reinterpret_cast<float*>(smem_raw);            // [dp][BM]
+    float* B_s = A_s + (size_t)dp * BM;                          // [STAGES][dp][BN]
+    float* L_s = B_s + (size_t)STAGES * dp * BN;                 // [BM][LCAP]
+    uint32_t* L_i = reinterpret_cast<uint32_t*>(L_s + BM * LCAP);
+    float* buf_s = reinterpret_cast<float*>(L_i + BM * LCAP);   // [BM][BUF]
+    uint32_t* buf_i = reinterpret_cast<uint32_t*>(buf_s + BM * BUF);
+    int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);       // [BM]
+    int* len_s = cnt_s + BM;                                     // [BM]
+    float* tau_s = reinterpret_cast<float*>(len_s + BM);         // [BM]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    // The block's 128 consecutive query rows, or 128 entries of a device-side row list.
+    const int q0 = blockIdx.x * BM;
+    const int nq = qlist ? min(BM, (int)*qcount - q0) : BM;
+    if (nq <= 0) return;
+    auto row_of = [&](int qi) -> int { return qlist ? (qi < nq ? (int)qlist[q0 + qi] : -1) : q0 + qi; };
+    const int ntiles = np / BN;
+
+    auto load_tile = [&](float* dst, int c0) {
+        for (int ch = tid; ch < dp * (BN / 4); ch += NT) {
+            const int t = ch / (BN / 4), c4 = ch % (BN / 4);
+            cp_async16(dst + t * BN + c4 * 4, xsT + (size_t)t * np + c0 + c4 * 4);
+        }
+    };
+    if (qlist) {
+        for (int e = tid; e < dp * BM; e += NT) {
+            const int t = e / BM, qi = e % BM;
+            A_s[t * BM + qi] = qi < nq ? xsT[(size_t)t * np + qlist[q0 + qi]] : 0.0f;
+        }
+    } else {
+        load_tile(A_s, q0);
+    }
+    load_tile(B_s, 0);
+    cp_async_commit();
+    if (ntiles > 1) load_tile(B_s + (size_t)dp * BN, BN);
+    cp_async_commit();
+    for (int q = tid; q < BM; q += NT) {
+        cnt_s[q] = 0;
+        len_s[q] = 0;
+        tau_s[q] = -CUDART_INF_F;
+    }
+    // Unfilled slots read back as column 0 with score −∞ (only possible with NaN input, which the
+    // host reports as an error): every index stays in range.
+    for (int e = tid; e < BM * LCAP; e += NT) {
+        L_s[e] = -CUDART_INF_F;
+        L_i[e] = 0u;
+    }
+
+    auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
+    auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
+
+    for (int tile = 0; tile < ntiles; ++tile) {
+        cp_async_wait<1>();
+        __syncthreads();  // tile's stage landed for every thread; stage (tile+2)%3 is free again
+        if (tile + 2 < ntiles) load_tile(B_s + (size_t)((tile + 2) % STAGES) * dp * BN, (tile + 2) * BN);
+        cp_async_commit();
+        const float* Bst = B_s + (size_t)(tile % STAGES) * dp * BN;
+        const int c0 = tile * BN;
+
+        float acc[8][8];
+#if COSTAL_FP32_PAIRED
+        // Blackwell's paired FP32 FMA: one instruction does two independent single-rounding FMAs,
+        // so the values are those of the scalar fmaf chain below.
+        unsigned long long acc2[8][4];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
+#pragma unroll(DPC ? DPC : 4)
+        for (int t = 0; t < dp; ++t) {
+            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
+            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
+            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const unsigned long long bp[4] = {pack2(b0.x, b0.y), pack2(b0.z, b0.w), pack2(b1.x, b1.y), pack2(b1.z, b1.w)};
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const unsigned long long ap = pack2(a[i], a[i]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc2[i][j] = ffma2(ap, bp[j], acc2[i][j]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
+#else
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+#pragma unroll(DPC ? DPC : 4)
+        for (int t = 0; t < dp; ++t) {
+            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
+            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
+            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
+            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+#endif
+
+        // Admission test against each query's τ at the tile start: a max-tree per register row.
+        bool hit = false;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float m01 = fmaxf(acc[i][0], acc[i][1]), m23 = fmaxf(acc[i][2], acc[i][3]);
+            const float m45 = fmaxf(acc[i][4], acc[i][5]), m67 = fmaxf(acc[i][6], acc[i][7]);
+            hit |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > tau_s[qi_of(i)];
+        }
+        if (hit) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const float th = tau_s[qi_of(i)];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (acc[i][j] > th) {
+                        const int qi = qi_of(i), col = c0 + cj_of(j);
+                        if (col < n && col != row_of(qi)) {
+                            const int pos = atomicAdd(&cnt_s[qi], 1);
+                            if (pos < BUF) {
+                                buf_s[qi * BUF + pos] = acc[i][j];
+                                buf_i[qi * BUF + pos] = (uint32_t)col;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (__any_sync(COSTAL_FULL_MASK, hit)) {
+            // Warp-local merge of this warp's 16 queries (8w..8w+7 and 64+8w..64+8w+7).
+            for (int qq = 0; qq < 16; ++qq) {
+                const int qi = qq < 8 ? 8 * warp + qq : 64 + 8 * warp + (qq - 8);
+                const int c = cnt_s[qi];
+                if (c == 0) continue;
+                const int q = row_of(qi);
+                float ls[SLOTS];
+                uint32_t li[SLOTS];
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    ls[s] = L_s[qi * LCAP + s * 32 + lane];
+                    li[s] = L_i[qi * LCAP + s * 32 + lane];
+                }
+                int len = len_s[qi];
+                if (c <= BUF) {
+                    for (int e = 0; e < c; ++e)
+                        list_insert<SLOTS>(ls, li, len, cap, buf_s[qi * BUF + e], buf_i[qi * BUF + e], lane);
+                } else {
+                    const float th0 = tau_s[qi];
+                    for (int cc = 0; cc < BN / 32; ++cc) {
+                        const int cl = cc * 32 + lane, col = c0 + cl;
+                        float sv = 0.0f;
+#pragma unroll(DPC ? DPC : 4)
+                        for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
+                        unsigned m = __ballot_sync(COSTAL_FULL_MASK, col < n && col != q && sv > th0);
+                        while (m) {
+                            const int src = __ffs(m) - 1;
+                            m &= m - 1;
+                            const float v = __shfl_sync(COSTAL_FULL_MASK, sv, src);
+                            list_insert<SLOTS>(ls, li, len, cap, v, (uint32_t)(c0 + cc * 32 + src), lane);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < SLOTS; ++s) {
+                    L_s[qi * LCAP + s * 32 + lane] = ls[s];
+                    L_i[qi * LCAP + s * 32 + lane] = li[s];
+                }
+                const float worst = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
+                __syncwarp();
+                if (lane == 0) {
+                    len_s[qi] = len;
+                    tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
+                    cnt_s[qi] = 0;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int e = tid; e < BM * cap; e += NT) {
+        const int qi = e / cap, p = e % cap, q = row_of(qi);
+        if (q >= 0 && q < n) {
+            cand_idx[(size_t)q * lstride + p] = L_i[qi * LCAP + p];
+            cand_score[(size_t)q * lstride + p] = L_s[qi * LCAP + p];
+        }
+    }
+    for (int qi = tid; qi < BM; qi += NT) {
+        const int q = row_of(qi);
+        if (q >= 0 && q < n) tau_out[q] = tau_s[qi];
+    }
+}
+
+size_t coarse_smem_bytes(int dp, int slots) {
+    const size_t lcap = 32 * (size_t)slots;
+    return (size_t)dp * BM * 4 + (size_t)STAGES * dp * BN * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 +
+           BM * 4 * 3;
+}
+
+template <int S, int D>
+cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                       const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
+    const size_t smem = coarse_smem_bytes(dp, S);
+    cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_coarse_fp32<S, D><<<np / BM, NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score,
+                                                   tau);
+    return cudaGetLastError();
+}
+
+template <int S>
+cudaError_t dispatch_d(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                       const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
+#define COSTAL_D(D) \
+    case D: return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+    switch (dp) {
+        COSTAL_D(8) COSTAL_D(16) COSTAL_D(24) COSTAL_D(32) COSTAL_D(40) COSTAL_D(48) COSTAL_D(56) COSTAL_D(64)
+        default: return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+    }
+#undef COSTAL_D
+}
+
+}  // namespace plain
+
+size_t coarse_fp32_smem(int dp, int cap) { return plain::coarse_smem_bytes(dp, coarse_slots(cap)); }
+
+int coarse_dpad(int d) { return d <= 64 ? ((d < 1 ? 1 : d) + 7) / 8 * 8 : (d + 3) / 4 * 4; }
+
+cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                               const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
+                               cudaStream_t st) {
+    switch (coarse_slots(cap)) {
+        case 1: return plain::dispatch_d<1>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+        case 2: return plain::dispatch_d<2>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+        case 4:
+            return plain::launch_one<4, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace costal

@@ -12,6 +12,8 @@ cudaError_t launch_prep(const float* x, int n, int d, int np, int dp, double* no
                         unsigned long long* bad_row, cudaStream_t st);
 cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cudaStream_t st);
 int coarse_slots(int cap);
+// d_pad of the working copy: a multiple of 8 up to 64 (compile-time tile depths), else of 4.
+int coarse_dpad(int d);
 size_t coarse_fp32_smem(int dp, int cap);
 // qlist/qcount (optional): run only the rows listed on the device (128 per CTA, grid sized for n).
 cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,

@@ -4,9 +4,7 @@
 //   k_prep      — knn.rs:315-323 row_norms64 (f64, dimension order) and knn.rs:420-436 the
 //                 L2-normalised f32 working copy, written transposed (d_pad × n_pad) for the tiles;
 //                 also knn.rs:325-342's non-finite check (first bad row).
-//   k_coarse    — knn.rs:603-660 + 758-875: every (query block × column tile) dot product in FP32
-//                 on the CUDA cores (tiles staged in shared memory by cp.async), fused with the
-//                 per-query top-cap selection by (score desc, index asc).
+//   (the FP32 coarse kernel, knn.rs:603-660 + 758-875, lives in coarse_fp32.cu)
 //   k_rescore   — knn.rs:688-720 + 746-753: f64 rescoring of the cap candidates, the sort, the
 //                 ε-certificate s_k > τ + (d+4)·2⁻²³, and (fused) the Tanimoto edge weight of
 //                 weight.rs:30-37 for the k survivors.
@@ -110,257 +108,6 @@ __global__ void k_row_l2_norms_f32(const float* __restrict__ x, int n, int d, fl
     }
     out[r] = sqrtf(s);
 }
-
-// =================================================================================================
-// k_coarse_fp32: FP32 tiles fused with per-query top-cap selection
-// =================================================================================================
-
-namespace plain {
-
-constexpr int BM = 128;  // query rows per CTA
-constexpr int BN = 128;  // columns per tile
-constexpr int NT = 256;  // threads: 16 × 16, each an 8 × 8 register tile
-constexpr int BUF = 16;  // pending admissions per query per tile before the overflow path
-
-// (score desc, index asc) on f32 coarse scores: the heap order of knn.rs:798-801, reversed.
-__device__ __forceinline__ bool better(float sa, uint32_t ia, float sb, uint32_t ib) {
-    return sa > sb || (sa == sb && ia < ib);
-}
-
-// Insert (sv, cv) into the warp-distributed sorted list (position p = s·32 + lane), keeping the
-// best `cap`. `len` is warp-uniform.
-template <int SLOTS>
-__device__ __forceinline__ void list_insert(float (&ls)[SLOTS], uint32_t (&li)[SLOTS], int& len, int cap,
-                                            float sv, uint32_t cv, int lane) {
-    if (len == cap) {
-        const float ws = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
-        const uint32_t wi = __shfl_sync(COSTAL_FULL_MASK, li[(cap - 1) >> 5], (cap - 1) & 31);
-        if (!better(sv, cv, ws, wi)) return;
-    }
-    int pos = 0;
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        const int p = s * 32 + lane;
-        const bool b = p < len && better(ls[s], li[s], sv, cv);
-        pos += __popc(__ballot_sync(COSTAL_FULL_MASK, b));
-    }
-    float ns[SLOTS];
-    uint32_t ni[SLOTS];
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        float up_s = __shfl_up_sync(COSTAL_FULL_MASK, ls[s], 1);
-        uint32_t up_i = __shfl_up_sync(COSTAL_FULL_MASK, li[s], 1);
-        if (s > 0) {
-            const float cs = __shfl_sync(COSTAL_FULL_MASK, ls[s > 0 ? s - 1 : 0], 31);
-            const uint32_t ci = __shfl_sync(COSTAL_FULL_MASK, li[s > 0 ? s - 1 : 0], 31);
-            if (lane == 0) {
-                up_s = cs;
-                up_i = ci;
-            }
-        }
-        const int p = s * 32 + lane;
-        ns[s] = p > pos ? up_s : (p == pos ? sv : ls[s]);
-        ni[s] = p > pos ? up_i : (p == pos ? cv : li[s]);
-    }
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        ls[s] = ns[s];
-        li[s] = ni[s];
-    }
-    len = len + 1 < cap ? len + 1 : cap;
-}
-
-template <int SLOTS>
-__global__ void __launch_bounds__(NT, 1)
-    k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp, int cap, int lstride,
-                  const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount,
-                  uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
-    constexpr int LCAP = 32 * SLOTS;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* A_s = reinterpret_cast<float*>(smem_raw);           // [dp][BM]
-    float* B_s = A_s + (size_t)dp * BM;                         // [2][dp][BN]
-    float* L_s = B_s + (size_t)2 * dp * BN;                     // [BM][LCAP]
-    uint32_t* L_i = reinterpret_cast<uint32_t*>(L_s + BM * LCAP);
-    float* buf_s = reinterpret_cast<float*>(L_i + BM * LCAP);  // [BM][BUF]
-    uint32_t* buf_i = reinterpret_cast<uint32_t*>(buf_s + BM * BUF);
-    int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);      // [BM]
-    int* len_s = cnt_s + BM;                                    // [BM]
-    float* tau_s = reinterpret_cast<float*>(len_s + BM);        // [BM]
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int tx = tid & 15, ty = tid >> 4;
-    // Query rows: the block's 128 consecutive rows, or 128 entries of a device-side row list (the
-    // rows a certificate sent back for an FP32 re-run).
-    const int q0 = blockIdx.x * BM;
-    const int nq = qlist ? min(BM, (int)*qcount - q0) : BM;
-    if (nq <= 0) return;
-    auto row_of = [&](int qi) -> int { return qlist ? (qi < nq ? (int)qlist[q0 + qi] : -1) : q0 + qi; };
-    const int ntiles = np / BN;
-
-    auto load_tile = [&](float* dst, int c0) {
-        for (int ch = tid; ch < dp * (BN / 4); ch += NT) {
-            const int t = ch / (BN / 4), c4 = ch % (BN / 4);
-            cp_async16(dst + t * BN + c4 * 4, xsT + (size_t)t * np + c0 + c4 * 4);
-        }
-    };
-    if (qlist) {
-        for (int e = tid; e < dp * BM; e += NT) {
-            const int t = e / BM, qi = e % BM;
-            A_s[t * BM + qi] = qi < nq ? xsT[(size_t)t * np + qlist[q0 + qi]] : 0.0f;
-        }
-    } else {
-        load_tile(A_s, q0);
-    }
-    load_tile(B_s, 0);
-    cp_async_commit();
-    if (ntiles > 1) load_tile(B_s + (size_t)dp * BN, BN);
-    cp_async_commit();
-    for (int q = tid; q < BM; q += NT) {
-        cnt_s[q] = 0;
-        len_s[q] = 0;
-        tau_s[q] = -CUDART_INF_F;
-    }
-    // Unfilled list slots read back as column 0 with score −∞ (only possible when the input holds
-    // NaN, which the host reports as an error; every index stays in range either way).
-    for (int e = tid; e < BM * LCAP; e += NT) {
-        L_s[e] = -CUDART_INF_F;
-        L_i[e] = 0u;
-    }
-
-    // Query row of register i, column of register j (two 4-wide halves 64 apart: conflict-free
-    // float4 shared-memory reads).
-    auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
-    auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
-
-    for (int tile = 0; tile < ntiles; ++tile) {
-        cp_async_wait<1>();
-        __syncthreads();
-        const float* Bst = B_s + (size_t)(tile & 1) * dp * BN;
-        const int c0 = tile * BN;
-
-        float acc[8][8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
-#pragma unroll 4
-        for (int t = 0; t < dp; ++t) {
-            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
-            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
-            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
-            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-
-        // Admission: strictly above the query's threshold at the start of the tile. Every column
-        // of an earlier tile has a smaller index than any column here, so this is the reference's
-        // strict `v > th` test (knn.rs:774-780) and keeps exactly the top-cap by (score, index).
-        float th[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) th[i] = tau_s[qi_of(i)];
-        bool hit = false;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) hit |= acc[i][j] > th[i];
-        if (hit) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (acc[i][j] > th[i]) {
-                        const int qi = qi_of(i), col = c0 + cj_of(j);
-                        if (col < n && col != row_of(qi)) {
-                            const int pos = atomicAdd(&cnt_s[qi], 1);
-                            if (pos < BUF) {
-                                buf_s[qi * BUF + pos] = acc[i][j];
-                                buf_i[qi * BUF + pos] = (uint32_t)col;
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        const int pending = __syncthreads_or(hit);
-
-        if (pending) {
-            // Merge: each warp owns BM/8 queries. Buffers that overflowed are discarded and the
-            // query's tile row is recomputed (same FMA order, so the same values) and inserted
-            // column by column.
-            for (int qq = 0; qq < BM / 8; ++qq) {
-                const int qi = warp * (BM / 8) + qq;
-                const int c = cnt_s[qi];
-                if (c == 0) continue;
-                const int q = row_of(qi);
-                float ls[SLOTS];
-                uint32_t li[SLOTS];
-#pragma unroll
-                for (int s = 0; s < SLOTS; ++s) {
-                    ls[s] = L_s[qi * LCAP + s * 32 + lane];
-                    li[s] = L_i[qi * LCAP + s * 32 + lane];
-                }
-                int len = len_s[qi];
-                if (c <= BUF) {
-                    for (int e = 0; e < c; ++e)
-                        list_insert<SLOTS>(ls, li, len, cap, buf_s[qi * BUF + e], buf_i[qi * BUF + e], lane);
-                } else {
-                    const float th0 = tau_s[qi];
-                    for (int cc = 0; cc < BN / 32; ++cc) {
-                        const int cl = cc * 32 + lane, col = c0 + cl;
-                        float sv = 0.0f;
-                        for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
-                        unsigned m = __ballot_sync(COSTAL_FULL_MASK, col < n && col != q && sv > th0);
-                        while (m) {
-                            const int src = __ffs(m) - 1;
-                            m &= m - 1;
-                            const float v = __shfl_sync(COSTAL_FULL_MASK, sv, src);
-                            list_insert<SLOTS>(ls, li, len, cap, v, (uint32_t)(c0 + cc * 32 + src), lane);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int s = 0; s < SLOTS; ++s) {
-                    L_s[qi * LCAP + s * 32 + lane] = ls[s];
-                    L_i[qi * LCAP + s * 32 + lane] = li[s];
-                }
-                const float worst = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
-                if (lane == 0) {
-                    len_s[qi] = len;
-                    tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
-                    cnt_s[qi] = 0;
-                }
-            }
-            __syncthreads();
-        }
-        if (tile + 2 < ntiles) load_tile(B_s + (size_t)(tile & 1) * dp * BN, (tile + 2) * BN);
-        cp_async_commit();
-    }
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int e = tid; e < BM * cap; e += NT) {
-        const int qi = e / cap, p = e % cap, q = row_of(qi);
-        if (q >= 0 && q < n) {
-            cand_idx[(size_t)q * lstride + p] = L_i[qi * LCAP + p];
-            cand_score[(size_t)q * lstride + p] = L_s[qi * LCAP + p];
-        }
-    }
-    for (int qi = tid; qi < BM; qi += NT) {
-        const int q = row_of(qi);
-        if (q >= 0 && q < n) tau_out[q] = tau_s[qi];
-    }
-}
-
-size_t coarse_smem_bytes(int dp, int slots) {
-    const size_t lcap = 32 * (size_t)slots;
-    return (size_t)dp * BM * 4 + 2ull * dp * BN * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 + BM * 4 * 3;
-}
-
-}  // namespace plain
 
 // =================================================================================================
 // k_rescore: f64 rescoring, sort, certificate, fused Tanimoto weight
@@ -592,31 +339,6 @@ cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cu
 }
 
 int coarse_slots(int cap) { return cap <= 32 ? 1 : (cap <= 64 ? 2 : (cap <= 128 ? 4 : 0)); }
-
-size_t coarse_fp32_smem(int dp, int cap) { return plain::coarse_smem_bytes(dp, coarse_slots(cap)); }
-
-cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                               const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
-                               cudaStream_t st) {
-    const int slots = coarse_slots(cap);
-    const size_t smem = plain::coarse_smem_bytes(dp, slots);
-    const int blocks = np / plain::BM;
-    cudaError_t e;
-#define COSTAL_COARSE(S)                                                                                    \
-    e = cudaFuncSetAttribute(plain::k_coarse_fp32<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    if (e != cudaSuccess) return e;                                                                         \
-    plain::k_coarse_fp32<S><<<blocks, plain::NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, \
-                                                                    cand_score, tau);
-    if (slots == 1) {
-        COSTAL_COARSE(1)
-    } else if (slots == 2) {
-        COSTAL_COARSE(2)
-    } else {
-        COSTAL_COARSE(4)
-    }
-#undef COSTAL_COARSE
-    return cudaGetLastError();
-}
 
 cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
                            const float* cand_score, const float* tau, const double* norms, const double* row_eps,
