@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "topk.cuh"
 
 namespace costal {
 namespace plain {
@@ -47,52 +48,6 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
     unsigned long long d;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
-}
-
-__device__ __forceinline__ bool better(float sa, uint32_t ia, float sb, uint32_t ib) {
-    return sa > sb || (sa == sb && ia < ib);
-}
-
-// Insert (sv, cv) into the warp-distributed sorted list (position p = s·32 + lane), keeping the best
-// `cap`. `len` is warp-uniform.
-template <int SLOTS>
-__device__ __forceinline__ void list_insert(float (&ls)[SLOTS], uint32_t (&li)[SLOTS], int& len, int cap, float sv,
-                                            uint32_t cv, int lane) {
-    if (len == cap) {
-        const float ws = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
-        const uint32_t wi = __shfl_sync(COSTAL_FULL_MASK, li[(cap - 1) >> 5], (cap - 1) & 31);
-        if (!better(sv, cv, ws, wi)) return;
-    }
-    int pos = 0;
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        const int p = s * 32 + lane;
-        pos += __popc(__ballot_sync(COSTAL_FULL_MASK, p < len && better(ls[s], li[s], sv, cv)));
-    }
-    float ns[SLOTS];
-    uint32_t ni[SLOTS];
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        float up_s = __shfl_up_sync(COSTAL_FULL_MASK, ls[s], 1);
-        uint32_t up_i = __shfl_up_sync(COSTAL_FULL_MASK, li[s], 1);
-        if (s > 0) {
-            const float cs = __shfl_sync(COSTAL_FULL_MASK, ls[s > 0 ? s - 1 : 0], 31);
-            const uint32_t ci = __shfl_sync(COSTAL_FULL_MASK, li[s > 0 ? s - 1 : 0], 31);
-            if (lane == 0) {
-                up_s = cs;
-                up_i = ci;
-            }
-        }
-        const int p = s * 32 + lane;
-        ns[s] = p > pos ? up_s : (p == pos ? sv : ls[s]);
-        ni[s] = p > pos ? up_i : (p == pos ? cv : li[s]);
-    }
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        ls[s] = ns[s];
-        li[s] = ni[s];
-    }
-    len = len + 1 < cap ? len + 1 : cap;
 }
 
 template <int SLOTS, int DPC>

@@ -12,10 +12,11 @@
 //   kernel    One CTA per 128 query rows (M = 128, one TMEM lane per query), column tiles of N = 256.
 //             Warp 4 streams B tiles with TMA (128-byte swizzle) into a ring of shared-memory
 //             stages; warp 5 issues the MMAs (one elected thread) into two 256-column TMEM
-//             accumulators; warps 0-3 read the accumulators back (tcgen05.ld, 32 columns at a time),
-//             reject whole 32-column chunks with a 3-input max tree against the query's threshold,
-//             and push the rare survivors into a per-query heap in shared memory (the reference's
-//             BlockHeaps order: score desc, index asc; strict `v > τ` admission, knn.rs:774-780).
+//             accumulators; warps 0-3 read the accumulators back (tcgen05.ld, 64 columns at a time,
+//             the next load in flight while one is scanned), reject whole slices with a 3-input max
+//             tree against the query's threshold, and append the rare survivors to per-query buffers
+//             that the warp flushes cooperatively into sorted per-query lists in shared memory
+//             (score desc, index asc; strict `v > τ` admission, knn.rs:774-780).
 //   bound     Every query row i gets a rigorous bound E_i on |coarse − exact cosine| (k_row_eps):
 //             split remainder ‖a_lo‖·max‖b_lo‖ + ‖a_hi+a_lo‖·max‖r_b‖ + ‖r_a‖·max‖b_hi+b_lo‖ + ‖r_a‖·max‖r_b‖
 //             (Cauchy–Schwarz), plus the tensor-core accumulation (K + 16)·2⁻²¹·Σ|products| (four
@@ -38,6 +39,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "knn_tc.h"
+#include "topk.cuh"
 
 namespace costal {
 namespace tc {
@@ -74,9 +76,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait: false (and the flag raised) if the phase never completes. Every 1024 polls the wait
 // also checks the global flag, so once any thread of any CTA has given up, every later wait of the
 // launch returns at once and the kernel drains in microseconds.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long* timeout_flag) {
+// Roles that are not the bottleneck (TMA, MMA issue) sleep between polls so that they do not take
+// issue slots from the epilogue warps that share their schedulers.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long* timeout_flag,
+                                          bool sleep) {
     for (long long i = 0; i < WAIT_LIMIT; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (sleep) __nanosleep(64);
         if ((i & 1023) == 1023 && *reinterpret_cast<volatile unsigned long long*>(timeout_flag)) return false;
     }
     atomicExch(timeout_flag, 1ull);
@@ -120,67 +126,51 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// 64 consecutive TMEM columns of this thread's lane (32x32b shape, 64 repetitions). The load is
+// asynchronous: the values may be read only after tmem_wait on the same registers.
+#define COSTAL_R8(i) "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), \
+                     "=r"(r[i + 6]), "=r"(r[i + 7])
+#define COSTAL_W8(i) "+r"(r[i]), "+r"(r[i + 1]), "+r"(r[i + 2]), "+r"(r[i + 3]), "+r"(r[i + 4]), "+r"(r[i + 5]), \
+                     "+r"(r[i + 6]), "+r"(r[i + 7])
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,"
+        "%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+        : COSTAL_R8(0), COSTAL_R8(8), COSTAL_R8(16), COSTAL_R8(24), COSTAL_R8(32), COSTAL_R8(40), COSTAL_R8(48),
+          COSTAL_R8(56)
+        : "r"(taddr)
+        : "memory");
+}
+// Wait for this thread's outstanding TMEM loads. The registers are in/out operands, so no use of
+// them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[64]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : COSTAL_W8(0), COSTAL_W8(8), COSTAL_W8(16), COSTAL_W8(24), COSTAL_W8(32), COSTAL_W8(40),
+                   COSTAL_W8(48), COSTAL_W8(56)
+                 :
+                 : "memory");
+}
+#undef COSTAL_R8
+#undef COSTAL_W8
+
+// 8 TMEM columns at a run-time column offset, loaded and waited for.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ float max3f(float a, float b, float c) {
     float r;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
-}
-
-// ---- the per-query heap (knn.rs:791-875), one per epilogue thread, [slot][query] in smem --------
-__device__ __forceinline__ bool worse(float sa, uint32_t ia, float sb, uint32_t ib) {
-    return sa < sb || (sa == sb && ia > ib);
-}
-
-__device__ __noinline__ void heap_push(float* hs, uint32_t* hi, int q, int cap, int& len, float score, uint32_t id) {
-#define HS(p) hs[(p) * BLOCK_M + q]
-#define HI(p) hi[(p) * BLOCK_M + q]
-    if (len < cap) {
-        int pos = len;
-        while (pos > 0) {
-            const int parent = (pos - 1) >> 1;
-            const float ps = HS(parent);
-            const uint32_t pi = HI(parent);
-            if (!worse(score, id, ps, pi)) break;
-            HS(pos) = ps;
-            HI(pos) = pi;
-            pos = parent;
-        }
-        HS(pos) = score;
-        HI(pos) = id;
-        ++len;
-        return;
-    }
-    if (!worse(HS(0), HI(0), score, id)) return;
-    int pos = 0;
-    for (;;) {
-        const int left = 2 * pos + 1;
-        if (left >= cap) break;
-        int w = left;
-        if (left + 1 < cap && worse(HS(left + 1), HI(left + 1), HS(left), HI(left))) w = left + 1;
-        if (!worse(HS(w), HI(w), score, id)) break;
-        HS(pos) = HS(w);
-        HI(pos) = HI(w);
-        pos = w;
-    }
-    HS(pos) = score;
-    HI(pos) = id;
-#undef HS
-#undef HI
 }
 
 struct __align__(8) Barriers {
@@ -192,19 +182,120 @@ struct __align__(8) Barriers {
     uint32_t tmem_base;
 };
 
+// Per-query candidate buffer: BCAP = 2·LCAP entries in shared memory, [entry][query] with a row
+// stride of BLOCK_M + 1 words (appends of 32 lanes and the warp's reads of one query are both free
+// of bank conflicts). Survivors are appended with predicated stores; when a buffer could overflow,
+// the warp sorts it cooperatively, keeps the best `cap` and raises τ to the cap-th score. Every
+// candidate outside a buffer scored ≤ τ when it was seen or evicted, and τ only grows.
+constexpr int BSTRIDE = BLOCK_M + 1;
+
+// Sort one query's buffer (cntL entries) and keep its best `cap` entries at positions 0..cap-1.
+template <int SL>
+__device__ __noinline__ void flush_one(float* B_s, uint32_t* B_i, int qL, int cntL, int cap, int lane, float* tau_out) {
+    float sc[SL];
+    uint32_t id[SL];
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+        const int p = s * 32 + lane;
+        sc[s] = p < cntL ? B_s[p * BSTRIDE + qL] : -CUDART_INF_F;
+        id[s] = p < cntL ? B_i[p * BSTRIDE + qL] : 0xffffffffu;
+    }
+    warp_sort_f32<SL>(sc, id, lane);
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+        const int p = s * 32 + lane;
+        if (p < cap) {
+            B_s[p * BSTRIDE + qL] = sc[s];
+            B_i[p * BSTRIDE + qL] = id[s];
+        }
+    }
+    const float t = __shfl_sync(COSTAL_FULL_MASK, sc[(cap - 1) >> 5], (cap - 1) & 31);
+    if (lane == 0) *tau_out = t;
+    __syncwarp();
+}
+
+// Flush every lane whose buffer holds more than `limit` entries.
+template <int SL>
+__device__ __forceinline__ void flush_full(float* B_s, uint32_t* B_i, float* tau_s, int qbase, int lane, int cap,
+                                           int limit, int& cnt, float& tau) {
+    unsigned pend = __ballot_sync(COSTAL_FULL_MASK, cnt > limit);
+    if (!pend) return;
+    __syncwarp();  // the lanes' appends are visible to the whole warp
+    while (pend) {
+        const int L = __ffs(pend) - 1;
+        pend &= pend - 1;
+        flush_one<SL>(B_s, B_i, qbase + L, __shfl_sync(COSTAL_FULL_MASK, cnt, L), cap, lane, &tau_s[qbase + L]);
+        if (lane == L) {
+            cnt = cap;
+            tau = tau_s[qbase + L];
+        }
+    }
+}
+
+__device__ __forceinline__ float max8(const uint32_t* r) {
+    const float a = max3f(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]));
+    const float b = max3f(__uint_as_float(r[3]), __uint_as_float(r[4]), __uint_as_float(r[5]));
+    return max3f(a, b, fmaxf(__uint_as_float(r[6]), __uint_as_float(r[7])));
+}
+
+// One 64-column slice held in registers: a per-lane 8-bit mask of the 8-column groups whose maximum
+// is above the lane's threshold, OR-ed over the warp. Returns the warp's mask.
+__device__ __forceinline__ unsigned slice_mask(const uint32_t (&r)[64], float tau) {
+    unsigned m = 0;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) m |= (max8(r + 8 * g) > tau ? 1u : 0u) << g;
+    return __reduce_or_sync(COSTAL_FULL_MASK, m);
+}
+
+// The 8-column groups of a slice that some lane of the warp needs: re-read each from TMEM (at a
+// run-time column) and append each lane's survivors (strictly above τ, in range, not the query
+// itself). Kept out of line: the rare path stays off the hot loop's instruction footprint.
+template <int SL>
+__device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb, int n, int q, int qi, int qbase,
+                                          int lane, int cap, int q_lo, float* B_s, uint32_t* B_i, float* tau_s,
+                                          int* cnt_io, float* tau_io) {
+    constexpr int BCAP = 32 * SL;
+    int cnt = *cnt_io;
+    float tau = *tau_io;
+    while (gmask) {
+        const int g = __ffs(gmask) - 1;
+        gmask &= gmask - 1;
+        float v[8];
+        tmem_ld8(taddr + (uint32_t)(8 * g), v);
+        const int c = cb + 8 * g;
+        const bool clean = c + 8 <= n && (c + 8 <= q_lo || c >= q_lo + 32);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int col = c + j;
+            if (v[j] > tau && (clean || (col < n && col != q))) {
+                B_s[cnt * BSTRIDE + qi] = v[j];
+                B_i[cnt * BSTRIDE + qi] = (uint32_t)col;
+                ++cnt;
+            }
+        }
+        flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, BCAP - 8, cnt, tau);
+    }
+    *cnt_io = cnt;
+    *tau_io = tau;
+}
+
+template <int SLOTS>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
                 int nkb, int ksteps, int stages, int cap, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
                 float* __restrict__ tau_out, unsigned long long* __restrict__ timeout_flag) {
+    constexpr int SL = 2 * SLOTS;  // buffer slots per lane in a flush: BCAP = 2·LCAP entries
+    constexpr int BCAP = 32 * SL;
     extern __shared__ unsigned char smem_raw[];
     // 1024-byte alignment for the swizzled tiles
     const uint32_t base_u32 = smem_u32(smem_raw);
     unsigned char* smem = smem_raw + ((1024 - (base_u32 & 1023)) & 1023);
     unsigned char* a_tile = smem;                                   // nkb × 16 KB
     unsigned char* b_tiles = a_tile + (size_t)nkb * A_KB_BYTES;     // stages × nkb × 32 KB
-    float* heap_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * nkb * B_KB_BYTES);  // [cap][128]
-    uint32_t* heap_i = reinterpret_cast<uint32_t*>(heap_s + (size_t)cap * BLOCK_M);
-    Barriers* bars = reinterpret_cast<Barriers*>(heap_i + (size_t)cap * BLOCK_M);
+    float* B_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * nkb * B_KB_BYTES);  // [BCAP][BSTRIDE]
+    uint32_t* B_i = reinterpret_cast<uint32_t*>(B_s + BCAP * BSTRIDE);
+    float* tau_s = reinterpret_cast<float*>(B_i + BCAP * BSTRIDE);  // [128] flush results
+    Barriers* bars = reinterpret_cast<Barriers*>(tau_s + BLOCK_M);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q0 = blockIdx.x * BLOCK_M;
@@ -242,7 +333,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int t = 0; t < ntiles; ++t) {
                 const int s = t % stages;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u;
-                if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag)) break;
+                if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) break;
                 mbar_expect_tx(&bars->b_full[s], b_bytes);
                 unsigned char* dst = b_tiles + (size_t)s * b_bytes;
                 for (int kb = 0; kb < nkb; ++kb)
@@ -252,14 +343,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     } else if (warp == EPI_WARPS + 1) {
         // ------------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            bool ok = mbar_wait(&bars->a_full, 0, timeout_flag);
+            bool ok = mbar_wait(&bars->a_full, 0, timeout_flag, true);
             tc_fence_after();
             const uint32_t a_base = smem_u32(a_tile);
             for (int t = 0; ok && t < ntiles; ++t) {
                 const int s = t % stages, buf = t & 1;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u, bph = (uint32_t)(t >> 1) & 1u;
-                if (!mbar_wait(&bars->t_empty[buf], bph ^ 1u, timeout_flag)) break;
-                if (!mbar_wait(&bars->b_full[s], ph, timeout_flag)) break;
+                if (!mbar_wait(&bars->t_empty[buf], bph ^ 1u, timeout_flag, true)) break;
+                if (!mbar_wait(&bars->b_full[s], ph, timeout_flag, true)) break;
                 tc_fence_after();
                 const uint32_t b_base = smem_u32(b_tiles + (size_t)s * b_bytes);
                 const uint32_t d = tmem + (uint32_t)(buf * BLOCK_N);
@@ -275,49 +366,64 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
     } else {
         // ------------------------------------------------------------------ epilogue (warps 0-3)
-        const int qi = warp * 32 + lane;  // TMEM lane = query row within the block
-        const int q = q0 + qi;
+        const int qbase = warp * 32;
+        const int qi = qbase + lane;  // TMEM lane = query row within the block
+        const int q = q0 + qi, q_lo = q0 + qbase;
         float tau = -CUDART_INF_F;
-        int len = 0;
-        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        int cnt = 0;
+        const uint32_t lane_addr = tmem + ((uint32_t)qbase << 16);
+        uint32_t ra[64], rb[64];
+        int cnt_m = 0;  // cnt and tau round-trip through these when the rare path runs
+        float tau_m = tau;
         for (int t = 0; t < ntiles; ++t) {
             const int buf = t & 1;
             const uint32_t bph = (uint32_t)(t >> 1) & 1u;
-            if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag)) break;
+            if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag, false)) break;
             tc_fence_after();
             const int c0 = t * BLOCK_N;
+            const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
+            // Four 64-column slices, as a two-step software pipeline: the next slice's TMEM load is
+            // in flight while one is scanned. A slice costs a max tree and a warp OR; only the
+            // 8-column groups some lane needs are re-read and scanned.
+            tmem_ld64(tb, ra);
+            tmem_wait(ra);
 #pragma unroll 1
-            for (int ch = 0; ch < BLOCK_N / 32; ++ch) {
-                float v[32];
-                tmem_ld32(lane_addr + (uint32_t)(buf * BLOCK_N + ch * 32), v);
-                float m[11];
-#pragma unroll
-                for (int j = 0; j < 10; ++j) m[j] = max3f(v[3 * j], v[3 * j + 1], v[3 * j + 2]);
-                m[10] = fmaxf(v[30], v[31]);
-                const float mm = max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]),
-                                       max3f(max3f(m[6], m[7], m[8]), m[9], m[10]));
-                if (mm > tau) {
-                    const int cb = c0 + ch * 32;
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (v[j] > tau) {
-                            const int col = cb + j;
-                            if (col < n && col != q) {
-                                heap_push(heap_s, heap_i, qi, cap, len, v[j], (uint32_t)col);
-                                tau = len < cap ? -CUDART_INF_F : heap_s[qi];
-                            }
-                        }
-                    }
+            for (int h = 0; h < 2; ++h) {
+                tmem_ld64(tb + (uint32_t)(128 * h + 64), rb);
+                unsigned gm = slice_mask(ra, tau);
+                if (gm) {
+                    cnt_m = cnt;
+                    tau_m = tau;
+                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h), c0 + 128 * h, n, q, qi, qbase, lane, cap, q_lo, B_s,
+                                     B_i, tau_s, &cnt_m, &tau_m);
+                    cnt = cnt_m;
+                    tau = tau_m;
                 }
+                tmem_wait(rb);
+                if (h == 0) tmem_ld64(tb + 128, ra);
+                gm = slice_mask(rb, tau);
+                if (gm) {
+                    cnt_m = cnt;
+                    tau_m = tau;
+                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h + 64), c0 + 128 * h + 64, n, q, qi, qbase, lane, cap,
+                                     q_lo, B_s, B_i, tau_s, &cnt_m, &tau_m);
+                    cnt = cnt_m;
+                    tau = tau_m;
+                }
+                if (h == 0) tmem_wait(ra);
             }
+            // every TMEM read of this accumulator is complete: hand it back to the MMA warp
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bars->t_empty[buf]);
         }
+        // final selection: every buffer sorted, best `cap` first
+        flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, 0, cnt, tau);
+        __syncwarp();
         if (q < n) {
             for (int p = 0; p < cap; ++p) {
-                cand_idx[(size_t)q * cap + p] = p < len ? heap_i[p * BLOCK_M + qi] : 0u;
-                cand_score[(size_t)q * cap + p] = p < len ? heap_s[p * BLOCK_M + qi] : -CUDART_INF_F;
+                cand_idx[(size_t)q * cap + p] = p < cnt ? B_i[p * BSTRIDE + qi] : 0u;
+                cand_score[(size_t)q * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
             }
             tau_out[q] = tau;
         }
@@ -396,11 +502,15 @@ __global__ void k_row_eps(const double* __restrict__ pnorm, const unsigned long 
 
 static int kpad(int d) { return (3 * d + KB - 1) / KB * KB; }
 
+static size_t fixed_smem(int nkb, int cap) {
+    const int bcap = cap <= 32 ? 64 : 128;
+    return 1024 + (size_t)nkb * A_KB_BYTES + (size_t)(BLOCK_M + 1) * bcap * 8 + (size_t)BLOCK_M * 4 + sizeof(Barriers);
+}
+
 bool supported(int d, int cap) {
-    if (d < 1 || 3 * d > 128 || cap < 1) return false;
+    if (d < 1 || 3 * d > 128 || cap < 1 || cap > 64) return false;
     const int nkb = kpad(d) / KB;
-    const size_t fixed = 1024 + (size_t)nkb * A_KB_BYTES + (size_t)cap * BLOCK_M * 8 + sizeof(Barriers);
-    return fixed + 2ull * nkb * B_KB_BYTES <= 227 * 1024;
+    return fixed_smem(nkb, cap) + 2ull * nkb * B_KB_BYTES <= 227 * 1024;
 }
 
 size_t workspace_bytes(int n, int d) {
@@ -486,16 +596,17 @@ cudaError_t launch_coarse(const Plan& plan, int cap, uint32_t* cand_idx, float* 
         return cudaErrorInvalidValue;
     const int nkb = plan.kp / KB;
     const int ksteps = (3 * plan.d + 15) / 16;
-    const size_t fixed = 1024 + (size_t)nkb * A_KB_BYTES + (size_t)cap * BLOCK_M * 8 + sizeof(Barriers);
+    const size_t fixed = fixed_smem(nkb, cap);
     int stages = 4;
     while (stages > 2 && fixed + (size_t)stages * nkb * B_KB_BYTES > 227 * 1024) --stages;
     const size_t smem = fixed + (size_t)stages * nkb * B_KB_BYTES;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_coarse_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
-    k_coarse_tc<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, cand_idx, cand_score,
-                                                 tau, timeout_flag);
+    auto kern = cap <= 32 ? k_coarse_tc<1> : k_coarse_tc<2>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, cand_idx, cand_score, tau,
+                                          timeout_flag);
     return cudaGetLastError();
 }
 
