@@ -101,8 +101,12 @@ def _check_knob(name, v):
 
 
 def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None, matmul=None, sort_by_norm=True,
-               prune=True, n_threads=None):
-    """lib.rs:113-167: exact kNN. Returns ((idx int32 (n,k), cos float64 (n,k), norms float64 (n,)), stats)."""
+               prune=True, n_threads=None, learned_prune=False):
+    """lib.rs:113-167: exact kNN. Returns ((idx int32 (n,k), cos float64 (n,k), norms float64 (n,)), stats).
+
+    GB300 addition: with matmul="bf16" and learned_prune=True, a model trained by _mlp_train on this
+    data skips column blocks whose bound is below its prediction (every skip is certified).
+    """
     x = _arr(x, np.float32, 2, "x")
     n, d = x.shape
     if n > np.iinfo(np.int32).max:
@@ -120,7 +124,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
     cos = np.empty((n, k), np.float64)
     norms = np.empty(n, np.float64)
     st = L.KnnStats()
-    o = _opts(sel, margin, row_block, col_block, _BACKENDS[matmul], sort_by_norm, prune)
+    o = _opts(sel, margin, row_block, col_block, _BACKENDS[matmul], sort_by_norm, prune, learned_prune)
     _call(L.lib().costal_knn_exact, _ptr(x), n, d, k, C.byref(o), _ptr(idx), _ptr(cos), _ptr(norms), C.byref(st))
     stats = {
         "fallback_rows": int(st.fallback_rows),
@@ -133,7 +137,10 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
         "blocks_total": int(st.blocks_total),
         # GB300-only counters
         "recomputed_rows": int(st.recomputed_rows),
+        "pruned_fallback_rows": int(st.pruned_fallback_rows),
         "max_coarse_err": float(st.max_coarse_err),
+        "ms_order": float(st.ms_order),
+        "ms_coarse": float(st.ms_coarse),
         "ms_total": float(st.ms_total),
     }
     return (idx.view(np.int32), cos, norms), stats
@@ -189,7 +196,7 @@ def _fuzzy_union(idx, w):
     return rows[:m].copy(), cols[:m].copy(), wout[:m].copy()
 
 
-def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_knn=False):
+def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_knn=False, learned_prune=False):
     """GB300 addition: the fused X -> kNN -> weights -> fuzzy union of _api.py:460-462 on the device.
 
     Returns (rows int32, cols int32, weights float64), plus (idx, cos, norms) and stats when
@@ -211,7 +218,7 @@ def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_kn
         cos = np.empty((n, k), np.float64)
         norms = np.empty(n, np.float64)
     st = L.KnnStats()
-    o = _opts("cosine", margin, None, None, _BACKENDS[matmul], True, True)
+    o = _opts("cosine", margin, None, None, _BACKENDS[matmul], True, True, learned_prune)
     _call(L.lib().costal_build_graph, _ptr(x), n, d, k, C.byref(o), wc, _ptr(rows), _ptr(cols), _ptr(wout),
           C.byref(m), _ptr(idx), _ptr(cos), _ptr(norms), C.byref(st))
     m = m.value
@@ -314,3 +321,61 @@ def tile_budget_bytes() -> int:
 def default_matmul() -> str:
     """lib.rs:442-446: name of the default coarse-pass backend."""
     return "fp32"
+
+
+# ---- the learned block-pruning model (GB300 addition; no counterpart in the reference) ----------
+
+def _mlp_train(x, k, *, sample=200_000, epochs=30, batch=2048, lr=2e-3, quantile=0.05, margin=None, seed=20241203):
+    """Train the k-th-neighbour-cosine model on x (labels from the plain FP32 path); it stays loaded.
+
+    Returns the training stats (loss, mean absolute error, coverage = share of rows predicted at or
+    below their exact k-th cosine, times)."""
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    o = L.MlpOpts()
+    o.sample, o.epochs, o.batch = int(sample), int(epochs), int(batch)
+    o.margin = 0xFFFFFFFF if margin is None else int(margin)
+    o.lr, o.quantile, o.seed = float(lr), float(quantile), int(seed)
+    st = L.MlpStats()
+    _call(L.lib().costal_mlp_train, _ptr(x), n, d, int(k), C.byref(o), C.byref(st))
+    return st.as_dict()
+
+
+def _mlp_get():
+    """The loaded model: (f32 master weights, d, k, quantile)."""
+    cnt, d, k, q = C.c_uint64(), C.c_uint32(), C.c_uint32(), C.c_float()
+    _call(L.lib().costal_mlp_get, None, 0, C.byref(cnt), C.byref(d), C.byref(k), C.byref(q))
+    params = np.empty(cnt.value, np.float32)
+    _call(L.lib().costal_mlp_get, _ptr(params), cnt.value, C.byref(cnt), C.byref(d), C.byref(k), C.byref(q))
+    return params, int(d.value), int(k.value), float(q.value)
+
+
+def _mlp_set(params, d, k, quantile=0.05):
+    """Load a model (e.g. from a checkpoint, or a constant predictor for an ablation)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    _call(L.lib().costal_mlp_set, _ptr(params), params.size, int(d), int(k), float(quantile))
+
+
+def _mlp_clear():
+    _call(L.lib().costal_mlp_clear)
+
+
+def _mlp_forward(params, feat):
+    """Test hook: the GPU forward pass for given weights and features (m, F)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    feat = np.ascontiguousarray(feat, dtype=np.float32)
+    m, F = feat.shape
+    out = np.empty(m, np.float32)
+    _call(L.lib().costal_mlp_forward, _ptr(params), F, _ptr(feat), m, _ptr(out))
+    return out
+
+
+def _mlp_gradient(params, feat, y, quantile):
+    """Test hook: the GPU gradient of the mean pinball loss for given weights, features and labels."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    feat = np.ascontiguousarray(feat, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    m, F = feat.shape
+    grad = np.empty(params.size, np.float32)
+    _call(L.lib().costal_mlp_gradient, _ptr(params), F, _ptr(feat), _ptr(y), m, float(quantile), _ptr(grad))
+    return grad

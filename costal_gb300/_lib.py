@@ -54,6 +54,35 @@ class KnnStats(C.Structure):
         ("ms_rescore", C.c_double),
         ("ms_fallback", C.c_double),
         ("ms_total", C.c_double),
+        ("ms_order", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class MlpOpts(C.Structure):
+    _fields_ = [
+        ("sample", C.c_uint32),
+        ("epochs", C.c_uint32),
+        ("batch", C.c_uint32),
+        ("margin", C.c_uint32),
+        ("lr", C.c_float),
+        ("quantile", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
+
+class MlpStats(C.Structure):
+    _fields_ = [
+        ("samples", C.c_uint64),
+        ("steps", C.c_uint64),
+        ("params", C.c_uint64),
+        ("loss", C.c_double),
+        ("mae", C.c_double),
+        ("coverage", C.c_double),
+        ("ms_labels", C.c_double),
+        ("ms_train", C.c_double),
     ]
 
     def as_dict(self):
@@ -78,6 +107,12 @@ SIGNATURES = {
     "costal_leiden_many": [U64, P, P, P, U64, P, U64, P, U64, DBL, I32, INT, P, STR, SZ],
     "costal_modularity": [U64, P, P, P, U64, P, DBL, P, STR, SZ],
     "costal_reweight_jaccard_device_noalloc": [P, U64, U32, P, P, STR, SZ],
+    "costal_mlp_train": [P, U64, U32, U32, P, P, STR, SZ],
+    "costal_mlp_get": [P, U64, P, P, P, P, STR, SZ],
+    "costal_mlp_set": [P, U64, U32, U32, C.c_float, STR, SZ],
+    "costal_mlp_clear": [STR, SZ],
+    "costal_mlp_forward": [P, U32, P, U64, P, STR, SZ],
+    "costal_mlp_gradient": [P, U32, P, P, U64, C.c_float, P, STR, SZ],
 }
 
 _lib = None

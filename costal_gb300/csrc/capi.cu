@@ -10,10 +10,13 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "costal_gb300.h"
 #include "kernels.h"
 #include "knn_tc.h"
+#include "mlp.h"
+#include "prune.h"
 
 namespace {
 
@@ -47,10 +50,12 @@ struct Context {
     std::string init_err;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};
     Misc* h_misc = nullptr;
     DevBuf x, norms, xsT, cand_idx, cand_score, tau, out_idx, out_cos, out_w, fb_rows, fb_minsim, misc;
-    DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows;
+    DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
+    DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
+    MlpState mlp;
 };
 
 Context& ctx() {
@@ -138,6 +143,29 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+constexpr int MLP_CHUNK = 262144;  // rows per feature/forward chunk at inference
+
+// Learned thresholds: the model's prediction for every row, then t_Q = min over each query block.
+cudaError_t mlp_predict_thresholds(Context& c, prune::Plan& pp, cudaStream_t s) {
+    const int n = pp.n, d = pp.d, F = c.mlp.F;
+    const int np = (n + 127) / 128 * 128;
+    cudaError_t e;
+    if ((e = ensure(c.mlp_feat, (size_t)std::min(n, MLP_CHUNK) * F * 4)) != cudaSuccess) return e;
+    if ((e = ensure(c.mlp_pred, (size_t)n * 4)) != cudaSuccess) return e;
+    if ((e = ensure(c.mlp_rows, (size_t)std::min(n, MLP_CHUNK) * 4)) != cudaSuccess) return e;
+    for (int r0 = 0; r0 < n; r0 += MLP_CHUNK) {
+        const int m = std::min(MLP_CHUNK, n - r0);
+        if ((e = launch_iota(c.mlp_rows.as<uint32_t>(), r0, m, s)) != cudaSuccess) return e;
+        if ((e = mlp::features(c.xsT.as<float>(), np, d, pp.centroids, pp.K, c.mlp_rows.as<uint32_t>(), m,
+                               c.mlp_feat.as<float>(), s)) != cudaSuccess)
+            return e;
+        if ((e = mlp::forward(c.mlp.params_bf, F, c.mlp_feat.as<float>(), m, c.mlp_pred.as<float>() + r0, s)) !=
+            cudaSuccess)
+            return e;
+    }
+    return mlp::block_min(c.mlp_pred.as<float>(), pp.perm, n, pp.tq, s);
+}
+
 // The kNN on device buffers. Everything is asynchronous on `s` except the final read of Misc.
 // d_w (optional): the Tanimoto weight of every output edge, fused into the rescoring.
 void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn_opts& o, uint32_t* d_idx,
@@ -159,6 +187,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaEventRecord(c.ev[0], s));
     CK(launch_prep(d_x, n, d, np, dp, d_norms, c.xsT.as<float>(), &dm->bad_row, s));
     CK(cudaEventRecord(c.ev[1], s));
+    CK(cudaEventRecord(c.ev[5], s));
     const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
     bool used_tc = false;
     if (tanimoto) {
@@ -173,30 +202,45 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         CK(ensure(c.cand_score, (size_t)n * cap * 4));
         CK(ensure(c.tau, (size_t)n * 4));
         const double eps = ((double)d + 4.0) * F32_EPS;  // knn.rs:185-187
-        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap)) {
+        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap) && prune::supported(d)) {
             used_tc = true;
+            // Locality order (k-means cells) and per-query-block column lists, nearest blocks first;
+            // with a learned threshold, blocks whose bound is below it are skipped.
+            CK(ensure(c.prune_ws, prune::workspace_bytes(n, d)));
+            prune::Plan pp{};
+            CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), n, np, d, s, pp));
+            const bool learned = o.learned_prune && c.mlp.ready && c.mlp.d == d && c.mlp.k == k;
+            if (learned) {
+                CK(mlp_predict_thresholds(c, pp, s));
+            } else {
+                pp.tq = nullptr;
+            }
+            CK(prune::build_lists(pp, &dm->blocks_skipped, s));
+            CK(cudaEventRecord(c.ev[5], s));
             CK(ensure(c.tc_ws, tc::workspace_bytes(n, d)));
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
-            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, s, plan));
-            CK(tc::launch_coarse(plan, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(),
-                                 &dm->timeout_flag, c.sm_count, s));
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, pp.perm, s, plan));
+            CK(tc::launch_coarse(plan, cap, pp.lists, pp.counts, pp.ncb, c.cand_idx.as<uint32_t>(),
+                                 c.cand_score.as<float>(), c.tau.as<float>(), &dm->timeout_flag, c.sm_count, s));
             CK(cudaEventRecord(c.ev[2], s));
-            // The split-BF16 certificate with its per-row bound; rows that fail it are listed in
-            // tc_rows, re-run by the FP32 coarse kernel and rescored with the FP32 bound, whose
-            // failures in turn take the full-row regather.
+            // The split-BF16 certificate with its per-row bound (and, with pruning, the skipped
+            // blocks' bound); rows that fail it are listed in tc_rows, re-run over ALL columns by the
+            // FP32 coarse kernel and rescored with the FP32 bound, whose failures in turn take the
+            // full-row regather.
             CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, plan.row_eps, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx,
-                              d_cos, d_w, c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
+                              c.tau.as<float>(), d_norms, plan.row_eps, learned ? pp.row_ub : nullptr,
+                              &dm->prune_fail_count, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx, d_cos, d_w,
+                              c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
                               &dm->max_err_bits, s));
             if (dp > 64 || coarse_fp32_smem(dp, cap) > 227 * 1024)
                 throw Fail{COSTAL_EUNSUPPORTED, "d too large for the FP32 re-run of uncertified rows"};
             CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, c.tc_rows.as<uint32_t>(), &dm->tc_fail_count,
                                   c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
             CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, nullptr, eps, cap < n - 1, 0, c.tc_rows.as<uint32_t>(),
-                              &dm->tc_fail_count, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
-                              &dm->fb_count, nullptr, s));
+                              c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0,
+                              c.tc_rows.as<uint32_t>(), &dm->tc_fail_count, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(),
+                              c.fb_minsim.as<double>(), &dm->fb_count, nullptr, s));
             CK(cudaEventRecord(c.ev[3], s));
         } else {
             if (dp > 64)
@@ -207,9 +251,9 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                                   c.cand_score.as<float>(), c.tau.as<float>(), s));
             CK(cudaEventRecord(c.ev[2], s));
             CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, nullptr, eps, cap < n - 1, 0, nullptr, nullptr, d_idx,
-                              d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->fb_count,
-                              &dm->max_err_bits, s));
+                              c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0, nullptr,
+                              nullptr, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
+                              &dm->fb_count, &dm->max_err_bits, s));
             CK(cudaEventRecord(c.ev[3], s));
         }
         if (cap < n - 1) {
@@ -239,7 +283,8 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         std::memcpy(&me, &hm.max_err_bits, 8);
         st->max_coarse_err = me;
         st->ms_prep = elapsed(c.ev[0], c.ev[1]);
-        st->ms_coarse = elapsed(c.ev[1], c.ev[2]);
+        st->ms_order = elapsed(c.ev[1], c.ev[5]);
+        st->ms_coarse = elapsed(c.ev[5], c.ev[2]);
         st->ms_rescore = elapsed(c.ev[2], c.ev[3]);
         st->ms_fallback = elapsed(c.ev[3], c.ev[4]);
         st->ms_total = elapsed(c.ev[0], c.ev[4]);
@@ -512,6 +557,217 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
         const costal_knn_opts o = opts ? *opts : defaults();
         cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
         run_build(c, d_x, n, d, k, o, weight, d_rows, d_cols, d_w, m, stats, s);
+    });
+}
+
+
+// ---- the learned block-pruning model ----------------------------------------------------------
+
+int costal_mlp_train(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_mlp_opts* mo,
+                     costal_mlp_stats* stats, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        if (!prune::supported((int)d)) throw Fail{COSTAL_EUNSUPPORTED, "learned pruning supports 1 <= d <= 64"};
+        costal_mlp_opts o{};
+        o.sample = 200000;
+        o.epochs = 30;
+        o.batch = 2048;
+        o.lr = 2e-3f;
+        o.quantile = 0.05f;
+        o.margin = UINT32_MAX;
+        o.seed = 20241203;
+        if (mo) o = *mo;
+        cudaStream_t s = c.stream;
+        const int N = (int)n, D = (int)d, K = (int)k;
+        const int dp = coarse_dpad(D), np = round_up(N, 128);
+        const uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
+        const int cap = (int)std::min<uint64_t>((uint64_t)k + margin, n - 1);
+        if (coarse_slots(cap) == 0 || coarse_fp32_smem(dp, cap) > 227 * 1024)
+            throw Fail{COSTAL_EUNSUPPORTED, "k + margin too large for the FP32 label pass"};
+        const int m = (int)std::min<uint64_t>(o.sample ? o.sample : n, n);
+        const int F = D + MLP_TOPC;
+        const size_t P = mlp_param_count(F);
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.norms, n * 8ull));
+        CK(ensure(c.xsT, (size_t)dp * np * 4));
+        CK(ensure(c.misc, sizeof(Misc)));
+        CK(ensure(c.cand_idx, (size_t)n * cap * 4));
+        CK(ensure(c.cand_score, (size_t)n * cap * 4));
+        CK(ensure(c.tau, n * 4ull));
+        CK(ensure(c.out_idx, n * k * 4ull));
+        CK(ensure(c.out_cos, n * k * 8ull));
+        CK(ensure(c.fb_rows, n * 4ull));
+        CK(ensure(c.fb_minsim, n * 8ull));
+        CK(ensure(c.mlp_rows, (size_t)std::max(m, std::min(N, MLP_CHUNK)) * 4));
+        CK(ensure(c.mlp_y, (size_t)m * 4));
+        CK(ensure(c.mlp_feat, (size_t)std::max(m, std::min(N, MLP_CHUNK)) * F * 4));
+        CK(ensure(c.mlp_pred, std::max<size_t>(n, m) * 4));
+        CK(ensure(c.mlp_params, P * 4));
+        CK(ensure(c.mlp_params_bf, P * 4));
+        CK(ensure(c.mlp_m1, P * 4));
+        CK(ensure(c.mlp_m2, P * 4));
+        CK(ensure(c.mlp_grad, P * 4));
+        CK(ensure(c.mlp_partial, (size_t)((o.batch + 31) / 32) * P * 4));
+        Misc* dm = c.misc.as<Misc>();
+        CK(cudaMemsetAsync(dm, 0, sizeof(Misc), s));
+        CK(cudaMemsetAsync(&dm->bad_row, 0xff, 8, s));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        CK(cudaEventRecord(c.ev[0], s));
+        CK(launch_prep(c.x.as<float>(), N, D, np, dp, c.norms.as<double>(), c.xsT.as<float>(), &dm->bad_row, s));
+        // the same cells (and so the same features) as the pruned kNN computes for this data
+        CK(ensure(c.prune_ws, prune::workspace_bytes(N, D)));
+        prune::Plan pp{};
+        CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), N, np, D, s, pp));
+        // labels: the exact k-th-neighbour cosine of every sampled row, from the plain FP32 path
+        uint32_t* rows = c.mlp_rows.as<uint32_t>();
+        CK(launch_stride_rows(rows, m, N, s));
+        unsigned hm = (unsigned)m;
+        CK(cudaMemcpyAsync(&dm->tc_fail_count, &hm, 4, cudaMemcpyHostToDevice, s));
+        CK(launch_coarse_fp32(c.xsT.as<float>(), N, np, dp, cap, cap, rows, &dm->tc_fail_count, c.cand_idx.as<uint32_t>(),
+                              c.cand_score.as<float>(), c.tau.as<float>(), s));
+        const double eps = ((double)d + 4.0) * F32_EPS;
+        CK(launch_rescore(c.x.as<float>(), N, D, K, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                          c.tau.as<float>(), c.norms.as<double>(), nullptr, nullptr, nullptr, eps, cap < N - 1, 0, rows,
+                          &dm->tc_fail_count, c.out_idx.as<uint32_t>(), c.out_cos.as<double>(), nullptr,
+                          c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->fb_count, nullptr, s));
+        if (cap < N - 1)
+            CK(launch_gather(c.x.as<float>(), c.xsT.as<float>(), N, np, D, dp, K, c.norms.as<double>(),
+                             c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->fb_count, 0, 0,
+                             std::min(N, 4 * c.sm_count), c.out_idx.as<uint32_t>(), c.out_cos.as<double>(), nullptr, s));
+        CK(launch_kth(c.out_cos.as<double>(), rows, m, K, c.mlp_y.as<float>(), s));
+        CK(mlp::features(c.xsT.as<float>(), np, D, pp.centroids, pp.K, rows, m, c.mlp_feat.as<float>(), s));
+        CK(cudaEventRecord(c.ev[1], s));
+        // Adam on the pinball loss, minibatches in sample order
+        CK(launch_init_params(c.mlp_params.as<float>(), F, (unsigned long long)o.seed, s));
+        CK(cudaMemsetAsync(c.mlp_m1.p, 0, P * 4, s));
+        CK(cudaMemsetAsync(c.mlp_m2.p, 0, P * 4, s));
+        int t = 0;
+        const int B = (int)std::max<uint32_t>(32, o.batch);
+        for (uint32_t ep = 0; ep < o.epochs; ++ep) {
+            for (int b0 = 0; b0 < m; b0 += B) {
+                const int mb = std::min(B, m - b0);
+                CK(mlp::gradient(c.mlp_params.as<float>(), F, c.mlp_feat.as<float>() + (size_t)b0 * F,
+                                 c.mlp_y.as<float>() + b0, mb, o.quantile, c.mlp_partial.as<float>(),
+                                 c.mlp_grad.as<float>(), s));
+                CK(mlp::adam(c.mlp_params.as<float>(), c.mlp_grad.as<float>(), c.mlp_m1.as<float>(),
+                             c.mlp_m2.as<float>(), P, o.lr, ++t, s));
+            }
+        }
+        CK(mlp::round_bf16(c.mlp_params.as<float>(), c.mlp_params_bf.as<float>(), P, s));
+        CK(mlp::forward(c.mlp_params_bf.as<float>(), F, c.mlp_feat.as<float>(), m, c.mlp_pred.as<float>(), s));
+        CK(cudaEventRecord(c.ev[2], s));
+        std::vector<float> pred(m), y(m);
+        CK(cudaMemcpyAsync(pred.data(), c.mlp_pred.p, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(y.data(), c.mlp_y.p, (size_t)m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (c.h_misc->bad_row != ~0ull)
+            throw Fail{COSTAL_EINVAL, "row " + std::to_string(c.h_misc->bad_row) + " contains NaN or inf"};
+        double loss = 0.0, mae = 0.0;
+        size_t below = 0;
+        for (int i = 0; i < m; ++i) {
+            const double r = (double)y[i] - (double)pred[i];
+            loss += r >= 0 ? o.quantile * r : (o.quantile - 1.0) * r;
+            mae += std::fabs(r);
+            below += pred[i] <= y[i];
+        }
+        c.mlp.ready = true;
+        c.mlp.d = D;
+        c.mlp.k = K;
+        c.mlp.F = F;
+        c.mlp.quantile = o.quantile;
+        c.mlp.params = c.mlp_params.as<float>();
+        c.mlp.params_bf = c.mlp_params_bf.as<float>();
+        c.mlp.nparams = P;
+        if (stats) {
+            stats->samples = (uint64_t)m;
+            stats->steps = (uint64_t)t;
+            stats->params = (uint64_t)P;
+            stats->loss = loss / m;
+            stats->mae = mae / m;
+            stats->coverage = (double)below / m;
+            stats->ms_labels = elapsed(c.ev[0], c.ev[1]);
+            stats->ms_train = elapsed(c.ev[1], c.ev[2]);
+        }
+    });
+}
+
+int costal_mlp_get(float* params, uint64_t capacity, uint64_t* count, uint32_t* d, uint32_t* k, float* quantile,
+                   char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (!c.mlp.ready) throw Fail{COSTAL_EINVAL, "no trained model"};
+        *count = c.mlp.nparams;
+        *d = (uint32_t)c.mlp.d;
+        *k = (uint32_t)c.mlp.k;
+        *quantile = c.mlp.quantile;
+        if (params && capacity >= c.mlp.nparams) {
+            CK(cudaMemcpy(params, c.mlp.params, c.mlp.nparams * 4, cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+int costal_mlp_set(const float* params, uint64_t count, uint32_t d, uint32_t k, float quantile, char* err,
+                   size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        const int F = (int)d + MLP_TOPC;
+        const size_t P = mlp_param_count(F);
+        if (!prune::supported((int)d) || count != P)
+            throw Fail{COSTAL_EINVAL, "parameter block does not match d (expected " + std::to_string(P) + " values)"};
+        CK(ensure(c.mlp_params, P * 4));
+        CK(ensure(c.mlp_params_bf, P * 4));
+        CK(cudaMemcpy(c.mlp_params.p, params, P * 4, cudaMemcpyHostToDevice));
+        CK(mlp::round_bf16(c.mlp_params.as<float>(), c.mlp_params_bf.as<float>(), P, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+        c.mlp.ready = true;
+        c.mlp.d = (int)d;
+        c.mlp.k = (int)k;
+        c.mlp.F = F;
+        c.mlp.quantile = quantile;
+        c.mlp.params = c.mlp_params.as<float>();
+        c.mlp.params_bf = c.mlp_params_bf.as<float>();
+        c.mlp.nparams = P;
+    });
+}
+
+int costal_mlp_clear(char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) { c.mlp.ready = false; });
+}
+
+int costal_mlp_forward(const float* params, uint32_t F, const float* feat, uint64_t m, float* out, char* err,
+                       size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (F < 1 || F > (uint32_t)MLP_MAXF) throw Fail{COSTAL_EINVAL, "F out of range"};
+        const size_t P = mlp_param_count((int)F);
+        cudaStream_t s = c.stream;
+        CK(ensure(c.mlp_grad, P * 4));
+        CK(ensure(c.mlp_feat, m * F * 4));
+        CK(ensure(c.mlp_pred, m * 4));
+        CK(cudaMemcpyAsync(c.mlp_grad.p, params, P * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c.mlp_feat.p, feat, m * F * 4, cudaMemcpyHostToDevice, s));
+        CK(mlp::forward(c.mlp_grad.as<float>(), (int)F, c.mlp_feat.as<float>(), (int)m, c.mlp_pred.as<float>(), s));
+        CK(cudaMemcpyAsync(out, c.mlp_pred.p, m * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, const float* y, uint64_t m,
+                        float quantile, float* grad, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (F < 1 || F > (uint32_t)MLP_MAXF) throw Fail{COSTAL_EINVAL, "F out of range"};
+        const size_t P = mlp_param_count((int)F);
+        cudaStream_t s = c.stream;
+        CK(ensure(c.mlp_m1, P * 4));
+        CK(ensure(c.mlp_grad, P * 4));
+        CK(ensure(c.mlp_feat, m * F * 4));
+        CK(ensure(c.mlp_y, m * 4));
+        CK(ensure(c.mlp_partial, ((m + 31) / 32) * P * 4));
+        CK(cudaMemcpyAsync(c.mlp_m1.p, params, P * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c.mlp_feat.p, feat, m * F * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c.mlp_y.p, y, m * 4, cudaMemcpyHostToDevice, s));
+        CK(mlp::gradient(c.mlp_m1.as<float>(), (int)F, c.mlp_feat.as<float>(), c.mlp_y.as<float>(), (int)m, quantile,
+                         c.mlp_partial.as<float>(), c.mlp_grad.as<float>(), s));
+        CK(cudaMemcpyAsync(grad, c.mlp_grad.p, P * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
     });
 }
 

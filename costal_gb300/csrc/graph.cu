@@ -35,6 +35,56 @@ cudaError_t launch_check_idx(const int32_t* idx, uint64_t nk, int n, unsigned lo
     return cudaGetLastError();
 }
 
+// ---- small utilities ------------------------------------------------------------------------------
+__global__ void k_iota(uint32_t* __restrict__ out, int start, int m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) out[i] = (uint32_t)(start + i);
+}
+cudaError_t launch_iota(uint32_t* out, int start, int m, cudaStream_t st) {
+    if (m > 0) k_iota<<<(m + 255) / 256, 256, 0, st>>>(out, start, m);
+    return cudaGetLastError();
+}
+// Evenly spaced sample rows: out[j] = ⌊j·n/m⌋.
+__global__ void k_stride_rows(uint32_t* __restrict__ out, int m, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) out[j] = (uint32_t)(((unsigned long long)j * (unsigned long long)n) / (unsigned long long)m);
+}
+cudaError_t launch_stride_rows(uint32_t* out, int m, int n, cudaStream_t st) {
+    if (m > 0) k_stride_rows<<<(m + 255) / 256, 256, 0, st>>>(out, m, n);
+    return cudaGetLastError();
+}
+// y[j] = cos[rows[j]·k + k − 1]: the k-th neighbour cosine of each listed row.
+__global__ void k_kth(const double* __restrict__ cos, const uint32_t* __restrict__ rows, int m, int k,
+                      float* __restrict__ y) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) y[j] = (float)cos[(size_t)rows[j] * k + k - 1];
+}
+cudaError_t launch_kth(const double* cos, const uint32_t* rows, int m, int k, float* y, cudaStream_t st) {
+    if (m > 0) k_kth<<<(m + 255) / 256, 256, 0, st>>>(cos, rows, m, k, y);
+    return cudaGetLastError();
+}
+// Deterministic He-uniform initialisation from a counter-based hash (SplitMix64 of seed + index).
+__global__ void k_init_params(float* __restrict__ P, int F, unsigned long long seed) {
+    const size_t np = (size_t)128 * F + 128 + (size_t)128 * 128 + 128 + 128 + 1;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (p + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const float u = (float)(z >> 40) / (float)(1ull << 24) * 2.0f - 1.0f;  // [-1, 1)
+        const size_t w1 = (size_t)128 * F, b1 = w1 + 128, w2 = b1 + (size_t)128 * 128, b2 = w2 + 128, w3 = b2 + 128;
+        float v = 0.0f;
+        if (p < w1) v = u * sqrtf(6.0f / (float)F);
+        else if (p >= b1 && p < w2) v = u * sqrtf(6.0f / 128.0f);
+        else if (p >= b2 && p < w3) v = u * sqrtf(6.0f / 128.0f);
+        P[p] = v;
+    }
+}
+cudaError_t launch_init_params(float* P, int F, unsigned long long seed, cudaStream_t st) {
+    k_init_params<<<64, 256, 0, st>>>(P, F, seed);
+    return cudaGetLastError();
+}
+
 // ---- Tanimoto weights --------------------------------------------------------------------------
 __global__ void k_tanimoto_w(const uint32_t* __restrict__ idx, const double* __restrict__ cos,
                              const double* __restrict__ norms, uint64_t nk, int k, double* __restrict__ out) {

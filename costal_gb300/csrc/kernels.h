@@ -21,7 +21,8 @@ cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap,
                                cudaStream_t st);
 cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
                            const float* cand_score, const float* tau, const double* norms, const double* row_eps,
-                           double eps, int certify, int select, const uint32_t* rlist, const unsigned* rcount,
+                           const double* row_ub, unsigned* ub_fail, double eps, int certify, int select,
+                           const uint32_t* rlist, const unsigned* rcount,
                            uint32_t* out_idx, double* out_cos, double* out_w, uint32_t* fb_rows, double* fb_minsim,
                            unsigned* fb_count, unsigned long long* max_err_bits, cudaStream_t st);
 int gather_capb(int k);
@@ -31,6 +32,10 @@ cudaError_t launch_gather(const float* x, const float* xsT, int n, int np, int d
                           int grid, uint32_t* out_idx, double* out_cos, double* out_w, cudaStream_t st);
 
 // ---- graph.cu ----------------------------------------------------------------------------------
+cudaError_t launch_iota(uint32_t* out, int start, int m, cudaStream_t st);
+cudaError_t launch_stride_rows(uint32_t* out, int m, int n, cudaStream_t st);
+cudaError_t launch_kth(const double* cos, const uint32_t* rows, int m, int k, float* y, cudaStream_t st);
+cudaError_t launch_init_params(float* P, int F, unsigned long long seed, cudaStream_t st);
 cudaError_t launch_check_idx(const int32_t* idx, uint64_t nk, int n, unsigned long long* first_bad, cudaStream_t st);
 cudaError_t launch_tanimoto_w(const uint32_t* idx, const double* cos, const double* norms, uint64_t nk, int k,
                               double* out, cudaStream_t st);

@@ -162,7 +162,8 @@ __global__ void __launch_bounds__(256)
     k_rescore(const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
               const uint32_t* __restrict__ cand_idx, const float* __restrict__ cand_score,
               const float* __restrict__ tau, const double* __restrict__ norms, const double* __restrict__ row_eps,
-              double eps, int certify, int select, const uint32_t* __restrict__ rlist,
+              const double* __restrict__ row_ub, unsigned* __restrict__ ub_fail, double eps, int certify, int select,
+              const uint32_t* __restrict__ rlist,
               const unsigned* __restrict__ rcount, uint32_t* __restrict__ out_idx, double* __restrict__ out_cos,
               double* __restrict__ out_w, uint32_t* __restrict__ fb_rows, double* __restrict__ fb_minsim,
               unsigned* __restrict__ fb_count, unsigned long long* __restrict__ max_err_bits) {
@@ -203,8 +204,11 @@ __global__ void __launch_bounds__(256)
     warp_sort<SLOTS>(sc, cs, id, lane);
     const double s_k = __shfl_sync(COSTAL_FULL_MASK, sc[(k - 1) >> 5], (k - 1) & 31);
     const double e = row_eps ? row_eps[i] : eps;
-    // knn.rs:704-714: with cap == n−1 nothing was left out; otherwise exact iff s_k > τ + ε.
-    if (certify && s_k <= __dadd_rn((double)tau[i], e)) {
+    // knn.rs:704-714: with cap == n−1 nothing was left out; otherwise exact iff s_k > τ + ε. With
+    // block pruning, every column of a skipped block scores at most row_ub: s_k must also beat it.
+    const bool ub_bad = row_ub && s_k <= row_ub[i];
+    if (ub_bad && lane == 0 && ub_fail) atomicAdd(ub_fail, 1u);
+    if ((certify && s_k <= __dadd_rn((double)tau[i], e)) || ub_bad) {
         if (lane == 0) {
             const unsigned slot = atomicAdd(fb_count, 1u);
             fb_rows[slot] = (uint32_t)i;
@@ -342,14 +346,16 @@ int coarse_slots(int cap) { return cap <= 32 ? 1 : (cap <= 64 ? 2 : (cap <= 128 
 
 cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
                            const float* cand_score, const float* tau, const double* norms, const double* row_eps,
-                           double eps, int certify, int select, const uint32_t* rlist, const unsigned* rcount,
+                           const double* row_ub, unsigned* ub_fail, double eps, int certify, int select,
+                           const uint32_t* rlist, const unsigned* rcount,
                            uint32_t* out_idx, double* out_cos, double* out_w, uint32_t* fb_rows, double* fb_minsim,
                            unsigned* fb_count, unsigned long long* max_err_bits, cudaStream_t st) {
     const int slots = coarse_slots(cap);
     const int blocks = (n + 7) / 8;
 #define COSTAL_RESCORE(S)                                                                                   \
     k_rescore<S><<<blocks, 256, 0, st>>>(x, n, d, k, cap, lstride, cand_idx, cand_score, tau, norms, row_eps, \
-                                         eps, certify, select, rlist, rcount, out_idx, out_cos, out_w, fb_rows, \
+                                         row_ub, ub_fail, eps, certify, select, rlist, rcount, out_idx, out_cos, \
+                                         out_w, fb_rows, \
                                          fb_minsim,                                                           \
                                          fb_count, max_err_bits);
     if (slots == 1) {

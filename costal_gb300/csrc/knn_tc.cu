@@ -238,6 +238,37 @@ __device__ __forceinline__ float max8(const uint32_t* r) {
     return max3f(a, b, fmaxf(__uint_as_float(r[6]), __uint_as_float(r[7])));
 }
 
+// The 8 group maxima of a 64-column slice.
+__device__ __forceinline__ void group_max8(const uint32_t (&r)[64], float* gm) {
+#pragma unroll
+    for (int g = 0; g < 8; ++g) gm[g] = max8(r + 8 * g);
+}
+
+// The cap-th largest of 32 values (cap ≤ 32): a bitonic sorting network in registers.
+__device__ __forceinline__ float kth_of_32(float (&v)[32], int cap) {
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const float a = v[i], b = v[j];
+                    const bool desc = (i & size) == 0;  // descending runs first
+                    v[i] = desc ? fmaxf(a, b) : fminf(a, b);
+                    v[j] = desc ? fminf(a, b) : fmaxf(a, b);
+                }
+            }
+        }
+    }
+    float t = v[0];
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+        if (i == cap - 1) t = v[i];
+    return t;
+}
+
 // One 64-column slice held in registers: a per-lane 8-bit mask of the 8-column groups whose maximum
 // is above the lane's threshold, OR-ed over the warp. Returns the warp's mask.
 __device__ __forceinline__ unsigned slice_mask(const uint32_t (&r)[64], float tau) {
@@ -282,8 +313,10 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
 template <int SLOTS>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
-                int nkb, int ksteps, int stages, int cap, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
-                float* __restrict__ tau_out, unsigned long long* __restrict__ timeout_flag) {
+                int nkb, int ksteps, int stages, int cap, const uint32_t* __restrict__ perm,
+                const uint32_t* __restrict__ lists, const uint32_t* __restrict__ counts, int ncb,
+                uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
+                unsigned long long* __restrict__ timeout_flag) {
     constexpr int SL = 2 * SLOTS;  // buffer slots per lane in a flush: BCAP = 2·LCAP entries
     constexpr int BCAP = 32 * SL;
     extern __shared__ unsigned char smem_raw[];
@@ -298,8 +331,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     Barriers* bars = reinterpret_cast<Barriers*>(tau_s + BLOCK_M);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Rows and columns are in the working order (rows sorted by locality cell; perm maps back to the
+    // original index). A CTA visits the column blocks of its list, nearest first, or all of them.
     const int q0 = blockIdx.x * BLOCK_M;
-    const int ntiles = np / BLOCK_N;
+    const int ntiles = lists ? (int)counts[blockIdx.x] : np / BLOCK_N;
+    const uint32_t* my_list = lists ? lists + (size_t)blockIdx.x * ncb : nullptr;
+    auto block_of = [&](int t) -> int { return my_list ? (int)my_list[t] : t; };
     const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb * B_KB_BYTES;
 
     if (threadIdx.x == 0) {
@@ -336,8 +373,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) break;
                 mbar_expect_tx(&bars->b_full[s], b_bytes);
                 unsigned char* dst = b_tiles + (size_t)s * b_bytes;
-                for (int kb = 0; kb < nkb; ++kb)
-                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KB, t * BLOCK_N, &bars->b_full[s]);
+                const int cb = block_of(t) * BLOCK_N;
+                for (int kb = 0; kb < nkb; ++kb) tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
             }
         }
     } else if (warp == EPI_WARPS + 1) {
@@ -380,8 +417,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t bph = (uint32_t)(t >> 1) & 1u;
             if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag, false)) break;
             tc_fence_after();
-            const int c0 = t * BLOCK_N;
+            const int c0 = block_of(t) * BLOCK_N;
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
+            if (t == 0 && cap <= 32) {
+                // A starting threshold from the first tile: the cap-th largest of its 32 column-group
+                // maxima is reached by cap distinct columns, so it is a valid lower bound of the
+                // query's cap-th score. The first tile itself is admitted at ≥ τ₀ (one below in the
+                // strict test), later tiles at > τ as usual.
+                float gmax[32];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    tmem_ld64(tb + (uint32_t)(64 * h), ra);
+                    tmem_wait(ra);
+                    group_max8(ra, gmax + 8 * h);
+                }
+                tau = nextafterf(kth_of_32(gmax, cap), -CUDART_INF_F);
+            }
             // Four 64-column slices, as a two-step software pipeline: the next slice's TMEM load is
             // in flight while one is scanned. A slice costs a max tree and a warp OR; only the
             // 8-column groups some lane needs are re-read and scanned.
@@ -421,11 +472,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, 0, cnt, tau);
         __syncwarp();
         if (q < n) {
+            const uint32_t qo = perm ? perm[q] : (uint32_t)q;
             for (int p = 0; p < cap; ++p) {
-                cand_idx[(size_t)q * cap + p] = p < cnt ? B_i[p * BSTRIDE + qi] : 0u;
-                cand_score[(size_t)q * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
+                const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0u;
+                cand_idx[(size_t)qo * cap + p] = perm ? perm[cw] : cw;
+                cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
             }
-            tau_out[q] = tau;
+            tau_out[qo] = tau;
         }
     }
     tc_fence_before();
@@ -440,17 +493,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 // One thread per padded row: split the normalised row (read from xsT) into the two operands and
 // record the f64 norms of its pieces: [0] ‖a_hi‖, [1] ‖a_lo‖, [2] ‖r‖, [3] ‖a_hi + a_lo‖.
-__global__ void k_split(const float* __restrict__ xsT, int n, int np, int d, int kp, __nv_bfloat16* __restrict__ opa,
-                        __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
+__global__ void k_split(const float* __restrict__ xsT, int n, int np, int d, int kp, const uint32_t* __restrict__ perm,
+                        __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
                         unsigned long long* __restrict__ colmax) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;  // working row
     if (r >= np) return;
+    const int o = r < n ? (perm ? (int)perm[r] : r) : 0;  // its original row
     __nv_bfloat16* ra = opa + (size_t)r * kp;
     __nv_bfloat16* rb = opb + (size_t)r * kp;
     double sh = 0.0, sl = 0.0, sr = 0.0, sp = 0.0;
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
     for (int t = 0; t < d; ++t) {
-        const float a = r < n ? xsT[(size_t)t * np + r] : 0.0f;
+        const float a = r < n ? xsT[(size_t)t * np + o] : 0.0f;
         const __nv_bfloat16 hb = __float2bfloat16_rn(a);
         const float h = __bfloat162float(hb);
         const float e = a - h;  // exact in f32
@@ -476,7 +530,7 @@ __global__ void k_split(const float* __restrict__ xsT, int n, int np, int d, int
     if (r < n) {
         const double v[4] = {sqrt(sh), sqrt(sl), sqrt(sr), sqrt(sp)};
         for (int j = 0; j < 4; ++j) {
-            pnorm[(size_t)j * n + r] = v[j];
+            pnorm[(size_t)j * n + o] = v[j];
             atomicMax(&colmax[j], (unsigned long long)__double_as_longlong(v[j]));
         }
     }
@@ -567,7 +621,8 @@ Layout carve(void* ws, int n, int d) {
 }
 }  // namespace
 
-cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, cudaStream_t st, Plan& plan) {
+cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, const uint32_t* perm, cudaStream_t st,
+                    Plan& plan) {
     (void)dp;
     const int np = (n + 255) / 256 * 256;  // the tensor tiles are 256 columns wide
     const int kp = kpad(d);
@@ -575,7 +630,7 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
     if (e != cudaSuccess) return e;
     // xsT has n_pad = ⌈n/128⌉·128 columns; rows in [n, np) are zero-filled by k_split itself.
-    k_split<<<(np + 127) / 128, 128, 0, st>>>(xsT, n, np_x, d, kp, L.opa, L.opb, L.pnorm, L.colmax);
+    k_split<<<(np + 127) / 128, 128, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax);
     k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps);
     plan.n = n;
     plan.d = d;
@@ -585,11 +640,13 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     plan.ops_b = L.opb;
     plan.row_eps = L.row_eps;
     plan.col_max = reinterpret_cast<const double*>(L.colmax);
+    plan.perm = perm;
     return cudaGetLastError();
 }
 
-cudaError_t launch_coarse(const Plan& plan, int cap, uint32_t* cand_idx, float* cand_score, float* tau,
-                          unsigned long long* timeout_flag, int sm_count, cudaStream_t st) {
+cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const uint32_t* counts, int ncb,
+                          uint32_t* cand_idx, float* cand_score, float* tau, unsigned long long* timeout_flag, int sm_count,
+                          cudaStream_t st) {
     (void)sm_count;
     CUtensorMap ma, mb;
     if (!make_map(&ma, plan.ops_a, plan.kp, plan.np, BLOCK_M) || !make_map(&mb, plan.ops_b, plan.kp, plan.np, BLOCK_N))
@@ -605,8 +662,8 @@ cudaError_t launch_coarse(const Plan& plan, int cap, uint32_t* cand_idx, float* 
     auto kern = cap <= 32 ? k_coarse_tc<1> : k_coarse_tc<2>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, cand_idx, cand_score, tau,
-                                          timeout_flag);
+    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, plan.perm, lists, counts,
+                                          ncb, cand_idx, cand_score, tau, timeout_flag);
     return cudaGetLastError();
 }
 

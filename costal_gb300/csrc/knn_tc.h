@@ -17,16 +17,20 @@ struct Plan {
     const void* ops_b;      // [np][kp] bf16 column operand  (hi | hi | lo)
     const double* row_eps;  // [n] certificate bound of each query row
     const double* col_max;  // [4] maxima over all rows of the split-residual norms
+    const uint32_t* perm;   // working -> original row (NULL: identity); operands are in working order
 };
 
 bool supported(int d, int cap);
 size_t workspace_bytes(int n, int d);
 // Split the normalised rows (xsT, d_pad × n_pad) into BF16 operands and per-row error norms, and
 // derive each row's certificate bound.
-cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, cudaStream_t st, Plan& plan);
+cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, const uint32_t* perm, cudaStream_t st,
+                    Plan& plan);
 // All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
-cudaError_t launch_coarse(const Plan& plan, int cap, uint32_t* cand_idx, float* cand_score, float* tau,
-                          unsigned long long* timeout_flag, int sm_count, cudaStream_t st);
+// With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]).
+cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const uint32_t* counts, int ncb,
+                          uint32_t* cand_idx, float* cand_score, float* tau, unsigned long long* timeout_flag, int sm_count,
+                          cudaStream_t st);
 
 }  // namespace tc
 }  // namespace costal

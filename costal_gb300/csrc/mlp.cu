@@ -1,0 +1,283 @@
+// The learned block-pruning model: features, forward, backward, Adam (all hand-written CUDA).
+//
+// Input of row i: its normalised coordinates (d values) and its 64 largest cosines to the 256
+// k-means centroids, sorted descending (the "distances to the 64 nearest centroids"). Network:
+// F = d + 64 → 128 (ReLU) → 128 (ReLU) → 1 (linear), predicting the row's k-th-neighbour cosine.
+// Training (costal_mlp_train) uses the pinball loss at a low quantile, so the prediction sits below
+// the true k-th score for most rows: it only sets a skip threshold, and every skip is certified
+// after the fact (a query whose k-th score does not beat its skipped blocks' bound is rescanned).
+// Inference runs in FP32 on bf16-rounded weights. Gradients are summed over fixed 32-row groups and
+// then over the groups in order, so training is deterministic.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "mlp.h"
+#include "topk.cuh"
+
+namespace costal {
+namespace mlp {
+
+constexpr int R = 32;    // rows per CTA
+constexpr int T = MLP_H; // threads per CTA (one per hidden unit)
+
+struct Off {
+    size_t w1, b1, w2, b2, w3, b3;
+};
+__host__ __device__ inline Off offsets(int F) {
+    Off o;
+    o.w1 = 0;
+    o.b1 = o.w1 + (size_t)MLP_H * F;
+    o.w2 = o.b1 + MLP_H;
+    o.b2 = o.w2 + (size_t)MLP_H * MLP_H;
+    o.w3 = o.b2 + MLP_H;
+    o.b3 = o.w3 + MLP_H;
+    return o;
+}
+
+// ---- features ---------------------------------------------------------------------------------
+// One warp per row: 8 centroid cosines per lane, a warp bitonic sort of the 256, the first 64 kept.
+__global__ void k_features(const float* __restrict__ xsT, int np, int d, const float* __restrict__ cent, int K,
+                           const uint32_t* __restrict__ rows, int m, float* __restrict__ feat) {
+    extern __shared__ float c_s[];  // [K][d]
+    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[e] = cent[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= m) return;
+    const uint32_t r = rows ? rows[i] : (uint32_t)i;
+    const int F = d + MLP_TOPC;
+    float sc[8];
+    uint32_t id[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int c = s * 32 + lane;
+        float dot = 0.0f;
+        if (c < K)
+            for (int t = 0; t < d; ++t) dot = fmaf(xsT[(size_t)t * np + r], c_s[c * d + t], dot);
+        sc[s] = c < K ? dot : -CUDART_INF_F;
+        id[s] = (uint32_t)c;
+    }
+    warp_sort_f32<8>(sc, id, lane);
+    float* f = feat + (size_t)i * F;
+    for (int t = lane; t < d; t += 32) f[t] = xsT[(size_t)t * np + r];
+    f[d + lane] = sc[0];
+    f[d + 32 + lane] = sc[1];
+}
+
+// ---- forward (shared by inference and training) ------------------------------------------------
+// CTA: R rows × T hidden units. Leaves h1, h2 in shared memory and returns the outputs in out_s.
+__device__ void forward_block(const float* __restrict__ P, int F, const float* __restrict__ feat, int m, int r0,
+                              float* f_s, float* h1_s, float* h2_s, float* out_s) {
+    const Off o = offsets(F);
+    const int j = threadIdx.x;
+    for (int e = j; e < R * F; e += T) {
+        const int r = e / F, t = e % F;
+        f_s[e] = r0 + r < m ? feat[(size_t)(r0 + r) * F + t] : 0.0f;
+    }
+    __syncthreads();
+    {
+        const float* w = P + o.w1 + (size_t)j * F;
+        const float b = P[o.b1 + j];
+        for (int r = 0; r < R; ++r) {
+            float z = b;
+            for (int t = 0; t < F; ++t) z = fmaf(w[t], f_s[r * F + t], z);
+            h1_s[r * T + j] = fmaxf(z, 0.0f);
+        }
+    }
+    __syncthreads();
+    {
+        const float* w = P + o.w2 + (size_t)j * MLP_H;
+        const float b = P[o.b2 + j];
+        for (int r = 0; r < R; ++r) {
+            float z = b;
+            for (int t = 0; t < MLP_H; ++t) z = fmaf(w[t], h1_s[r * T + t], z);
+            h2_s[r * T + j] = fmaxf(z, 0.0f);
+        }
+    }
+    __syncthreads();
+    if (j < R) {
+        float z = P[o.b3];
+        for (int t = 0; t < MLP_H; ++t) z = fmaf(P[o.w3 + t], h2_s[j * T + t], z);
+        out_s[j] = z;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(T) k_forward(const float* __restrict__ P, int F, const float* __restrict__ feat, int m,
+                                               float* __restrict__ out) {
+    extern __shared__ float sm[];
+    float* f_s = sm;                  // [R][F]
+    float* h1_s = f_s + R * F;        // [R][T]
+    float* h2_s = h1_s + R * T;       // [R][T]
+    float* out_s = h2_s + R * T;      // [R]
+    const int r0 = blockIdx.x * R;
+    forward_block(P, F, feat, m, r0, f_s, h1_s, h2_s, out_s);
+    if (threadIdx.x < R && r0 + threadIdx.x < m) out[r0 + threadIdx.x] = out_s[threadIdx.x];
+}
+
+// ---- backward ----------------------------------------------------------------------------------
+// Per CTA: forward, the pinball-loss gradient of its rows (mean over all m rows), and the gradient
+// of every parameter summed over the CTA's rows in row order → partial[blockIdx.x][nparams].
+__global__ void __launch_bounds__(T) k_grad_partial(const float* __restrict__ P, int F, const float* __restrict__ feat,
+                                                    const float* __restrict__ y, int m, float quantile,
+                                                    float* __restrict__ partial) {
+    extern __shared__ float sm[];
+    float* f_s = sm;                  // [R][F]
+    float* h1_s = f_s + R * F;        // [R][T]
+    float* h2_s = h1_s + R * T;       // [R][T]
+    float* out_s = h2_s + R * T;      // [R]
+    float* g_s = out_s + R;           // [R] dL/dout
+    float* dz2_s = g_s + R;           // [R][T]
+    float* dz1_s = dz2_s + R * T;     // [R][T]
+    const Off o = offsets(F);
+    const int j = threadIdx.x;
+    const int r0 = blockIdx.x * R;
+    forward_block(P, F, feat, m, r0, f_s, h1_s, h2_s, out_s);
+    if (j < R) {
+        const int i = r0 + j;
+        // pinball loss ρ(y − out): d/dout = (1 − α) when out > y, −α otherwise
+        g_s[j] = i < m ? (out_s[j] > y[i] ? 1.0f - quantile : -quantile) / (float)m : 0.0f;
+    }
+    __syncthreads();
+    float* G = partial + (size_t)blockIdx.x * mlp_param_count(F);
+    const float w3j = P[o.w3 + j];
+    {
+        float gw3 = 0.0f;
+        for (int r = 0; r < R; ++r) {
+            gw3 = fmaf(g_s[r], h2_s[r * T + j], gw3);
+            dz2_s[r * T + j] = h2_s[r * T + j] > 0.0f ? g_s[r] * w3j : 0.0f;
+        }
+        G[o.w3 + j] = gw3;
+        if (j == 0) {
+            float gb3 = 0.0f;
+            for (int r = 0; r < R; ++r) gb3 += g_s[r];
+            G[o.b3] = gb3;
+        }
+    }
+    __syncthreads();
+    {
+        // layer 2: dW2[j][t] = Σ_r dz2[r][j] h1[r][t], db2[j] = Σ_r dz2[r][j]
+        float gb = 0.0f;
+        for (int r = 0; r < R; ++r) gb += dz2_s[r * T + j];
+        G[o.b2 + j] = gb;
+        for (int t = 0; t < MLP_H; ++t) {
+            float s = 0.0f;
+            for (int r = 0; r < R; ++r) s = fmaf(dz2_s[r * T + j], h1_s[r * T + t], s);
+            G[o.w2 + (size_t)j * MLP_H + t] = s;
+        }
+        // dh1[r][j] = Σ_u dz2[r][u] W2[u][j], masked by the ReLU of layer 1
+        for (int r = 0; r < R; ++r) {
+            float s = 0.0f;
+            for (int u = 0; u < MLP_H; ++u) s = fmaf(dz2_s[r * T + u], P[o.w2 + (size_t)u * MLP_H + j], s);
+            dz1_s[r * T + j] = h1_s[r * T + j] > 0.0f ? s : 0.0f;
+        }
+    }
+    __syncthreads();
+    {
+        float gb = 0.0f;
+        for (int r = 0; r < R; ++r) gb += dz1_s[r * T + j];
+        G[o.b1 + j] = gb;
+        for (int t = 0; t < F; ++t) {
+            float s = 0.0f;
+            for (int r = 0; r < R; ++r) s = fmaf(dz1_s[r * T + j], f_s[r * F + t], s);
+            G[o.w1 + (size_t)j * F + t] = s;
+        }
+    }
+}
+
+__global__ void k_grad_reduce(const float* __restrict__ partial, int groups, size_t np, float* __restrict__ grad) {
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int g = 0; g < groups; ++g) s += partial[(size_t)g * np + p];
+        grad[p] = s;
+    }
+}
+
+__global__ void k_adam(float* __restrict__ P, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
+                       size_t np, float lr, float bc1, float bc2) {
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
+        const float gp = g[p];
+        const float a = 0.9f * m1[p] + 0.1f * gp;
+        const float b = 0.999f * m2[p] + 0.001f * gp * gp;
+        m1[p] = a;
+        m2[p] = b;
+        P[p] -= lr * (a / bc1) / (sqrtf(b / bc2) + 1e-8f);
+    }
+}
+
+__global__ void k_round_bf16(const float* __restrict__ P, float* __restrict__ Q, size_t np) {
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x)
+        Q[p] = __bfloat162float(__float2bfloat16_rn(P[p]));
+}
+
+__global__ void k_block_min(const float* __restrict__ pred, const uint32_t* __restrict__ perm, int n,
+                            float* __restrict__ tq) {
+    const int Q = blockIdx.x;
+    __shared__ float red[prune::QB];
+    const int w = Q * prune::QB + threadIdx.x;
+    red[threadIdx.x] = w < n ? pred[perm[w]] : CUDART_INF_F;
+    __syncthreads();
+    for (int s = prune::QB / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) red[threadIdx.x] = fminf(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tq[Q] = red[0];
+}
+
+// ---- launchers ----------------------------------------------------------------------------------
+
+static size_t fwd_smem(int F) { return (size_t)(R * F + 2 * R * T + R) * 4; }
+static size_t grad_smem(int F) { return (size_t)(R * F + 4 * R * T + 2 * R) * 4; }
+
+cudaError_t features(const float* xsT, int np, int d, const float* centroids, int K, const uint32_t* rows, int m,
+                     float* feat, cudaStream_t st) {
+    if (m == 0) return cudaSuccess;
+    const size_t smem = (size_t)K * d * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_features<<<(m + 7) / 8, 256, smem, st>>>(xsT, np, d, centroids, K, rows, m, feat);
+    return cudaGetLastError();
+}
+
+cudaError_t forward(const float* params, int F, const float* feat, int m, float* out, cudaStream_t st) {
+    if (m == 0) return cudaSuccess;
+    const size_t smem = fwd_smem(F);
+    cudaError_t e = cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_forward<<<(m + R - 1) / R, T, smem, st>>>(params, F, feat, m, out);
+    return cudaGetLastError();
+}
+
+cudaError_t gradient(const float* params, int F, const float* feat, const float* y, int m, float quantile,
+                     float* partial, float* grad, cudaStream_t st) {
+    const int groups = (m + R - 1) / R;
+    const size_t smem = grad_smem(F);
+    cudaError_t e = cudaFuncSetAttribute(k_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_grad_partial<<<groups, T, smem, st>>>(params, F, feat, y, m, quantile, partial);
+    k_grad_reduce<<<128, 256, 0, st>>>(partial, groups, mlp_param_count(F), grad);
+    return cudaGetLastError();
+}
+
+cudaError_t adam(float* params, const float* grad, float* m1, float* m2, size_t np, float lr, int t, cudaStream_t st) {
+    const float bc1 = 1.0f - powf(0.9f, (float)t), bc2 = 1.0f - powf(0.999f, (float)t);
+    k_adam<<<128, 256, 0, st>>>(params, grad, m1, m2, np, lr, bc1, bc2);
+    return cudaGetLastError();
+}
+
+cudaError_t round_bf16(const float* params, float* params_bf, size_t np, cudaStream_t st) {
+    k_round_bf16<<<64, 256, 0, st>>>(params, params_bf, np);
+    return cudaGetLastError();
+}
+
+cudaError_t block_min(const float* pred_orig, const uint32_t* perm, int n, float* tq, cudaStream_t st) {
+    k_block_min<<<(n + prune::QB - 1) / prune::QB, prune::QB, 0, st>>>(pred_orig, perm, n, tq);
+    return cudaGetLastError();
+}
+
+}  // namespace mlp
+}  // namespace costal

@@ -1,0 +1,438 @@
+// Locality order and block pruning for the tensor-core coarse pass.
+//
+// The reference visits column blocks in index order and prunes only for Tanimoto selection, by norm
+// windows (crates/costal-core/src/knn.rs:603-644, :272-283). This file gives the cosine path the same
+// two levers, with bounds that hold for the exact scores:
+//
+//   cells     spherical k-means (K = 256 centroids, a seeded sample of rows, a few Lloyd steps with
+//             deterministic centroid sums) and the cell of every row;
+//   order     a working order: rows stably sorted by cell (ties by original index). The tensor
+//             operands are laid out in this order; candidates are mapped back to original indices.
+//   geometry  for every 128-row query block Q and every 256-row column block B (in working order) a
+//             unit centre c and an angular radius r = max angle(row, c), in f64;
+//   bound     for q ∈ Q, x ∈ B: angle(q, x) ≥ angle(c_Q, c_B) − r_Q − r_B (the angle is a metric on
+//             the sphere), so cos(q, x) ≤ UB(Q, B) = cos(max(0, angle(c_Q, c_B) − r_Q − r_B − ξ)),
+//             with ξ = 1e-6 rad covering the f32 rounding of the normalised rows (≤ 1e-7 rad) and the
+//             f64 evaluation;
+//   lists     for every Q, the column blocks with UB ≥ t_Q, sorted by UB descending (the closest
+//             blocks first, so a query's threshold rises to its final value within the first tiles),
+//             and ub_skip[Q] = the largest UB of a skipped block. A query is certified only if its
+//             k-th exact score is strictly above ub_skip of its block; otherwise it is rescanned.
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "prune.h"
+
+namespace costal {
+namespace prune {
+
+constexpr int KM_BLOCK = 128;
+
+// ---- k-means ----------------------------------------------------------------------------------
+
+// Rows of xsT (d × np, transposed) listed in `rows` → a row-major [m][d] copy.
+__global__ void k_gather_rows(const float* __restrict__ xsT, int np, int d, const uint32_t* __restrict__ rows, int m,
+                              float* __restrict__ out) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * d; e += gridDim.x * blockDim.x) {
+        const int i = e / d, t = e % d;
+        out[e] = xsT[(size_t)t * np + rows[i]];
+    }
+}
+
+// Best centroid (largest dot with the unit centroid) of every row; rows are either a row-major
+// [m][d] array (rows_rm) or the columns of xsT. Centroids live in shared memory.
+__global__ void __launch_bounds__(KM_BLOCK) k_assign(const float* __restrict__ rows_rm, const float* __restrict__ xsT,
+                                                     int np, int m, int d, const float* __restrict__ cent, int K,
+                                                     uint32_t* __restrict__ assign) {
+    extern __shared__ float c_s[];  // [K][d]
+    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[e] = cent[e];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    float x[64];
+#pragma unroll
+    for (int t = 0; t < 64; ++t)
+        if (t < d) x[t] = rows_rm ? rows_rm[(size_t)i * d + t] : xsT[(size_t)t * np + i];
+    float best = -CUDART_INF_F;
+    uint32_t arg = 0;
+    for (int c = 0; c < K; ++c) {
+        float s = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 64; ++t)
+            if (t < d) s = fmaf(x[t], c_s[c * d + t], s);
+        if (s > best) {
+            best = s;
+            arg = (uint32_t)c;
+        }
+    }
+    assign[i] = arg;
+}
+
+// One CTA per centroid: the normalised sum of its rows. Thread t adds rows t, t+128, … in order,
+// then the 128 partial sums are combined by a fixed tree: deterministic. An empty cluster keeps its
+// previous centroid.
+constexpr int UPD_T = 128;
+__global__ void __launch_bounds__(UPD_T) k_centroid_update(const float* __restrict__ rows, int m, int d,
+                                                           const uint32_t* __restrict__ assign, float* __restrict__ cent) {
+    __shared__ float part[UPD_T][65];
+    __shared__ int cnt_s[UPD_T];
+    const int c = blockIdx.x;
+    float acc[64];
+#pragma unroll
+    for (int t = 0; t < 64; ++t) acc[t] = 0.0f;
+    int cnt = 0;
+    for (int i = threadIdx.x; i < m; i += UPD_T) {
+        if (assign[i] == (uint32_t)c) {
+            ++cnt;
+#pragma unroll
+            for (int t = 0; t < 64; ++t)
+                if (t < d) acc[t] += rows[(size_t)i * d + t];
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < 64; ++t)
+        if (t < d) part[threadIdx.x][t] = acc[t];
+    cnt_s[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int s = UPD_T / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            for (int t = 0; t < d; ++t) part[threadIdx.x][t] += part[threadIdx.x + s][t];
+            cnt_s[threadIdx.x] += cnt_s[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (cnt_s[0] == 0) return;
+    __shared__ float nrm;
+    if (threadIdx.x == 0) {
+        double nn = 0.0;
+        for (int t = 0; t < d; ++t) nn += (double)part[0][t] * part[0][t];
+        nrm = (float)sqrt(nn);
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < d && nrm > 0.0f) cent[(size_t)c * d + threadIdx.x] = part[0][threadIdx.x] / nrm;
+}
+
+// ---- working order: stable counting sort of rows by cell -------------------------------------
+
+constexpr int CHUNK = 1024;
+
+__global__ void k_cell_hist(const uint32_t* __restrict__ cell, int n, int K, uint32_t* __restrict__ hist) {
+    // one thread per chunk, sequential over its rows (deterministic)
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nch = (n + CHUNK - 1) / CHUNK;
+    if (ch >= nch) return;
+    uint32_t* h = hist + (size_t)ch * K;
+    for (int c = 0; c < K; ++c) h[c] = 0;
+    const int end = min(n, (ch + 1) * CHUNK);
+    for (int i = ch * CHUNK; i < end; ++i) h[cell[i]] += 1;
+}
+
+// Exclusive offsets in (cell, chunk) order: thread c totals its cell over the chunks, one warp
+// scans the K totals, then thread c rewrites its column of the histogram as offsets.
+__global__ void k_cell_scan(uint32_t* __restrict__ hist, int nch, int K, uint32_t* __restrict__ cell_start) {
+    __shared__ uint32_t tot[1024];
+    const int c = threadIdx.x;
+    uint32_t s = 0;
+    if (c < K)
+        for (int ch = 0; ch < nch; ++ch) s += hist[(size_t)ch * K + c];
+    tot[c] = s;
+    __syncthreads();
+    if (c == 0) {
+        uint32_t acc = 0;
+        for (int j = 0; j < K; ++j) {
+            const uint32_t v = tot[j];
+            tot[j] = acc;
+            acc += v;
+        }
+        cell_start[K] = acc;
+    }
+    __syncthreads();
+    if (c < K) {
+        uint32_t acc = tot[c];
+        cell_start[c] = acc;
+        for (int ch = 0; ch < nch; ++ch) {
+            const uint32_t v = hist[(size_t)ch * K + c];
+            hist[(size_t)ch * K + c] = acc;
+            acc += v;
+        }
+    }
+}
+
+__global__ void k_cell_scatter(const uint32_t* __restrict__ cell, int n, int K, uint32_t* __restrict__ hist,
+                               uint32_t* __restrict__ perm) {
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nch = (n + CHUNK - 1) / CHUNK;
+    if (ch >= nch) return;
+    uint32_t* h = hist + (size_t)ch * K;
+    const int end = min(n, (ch + 1) * CHUNK);
+    for (int i = ch * CHUNK; i < end; ++i) perm[h[cell[i]]++] = (uint32_t)i;
+}
+
+// ---- block geometry -------------------------------------------------------------------------------
+
+// One CTA per block of `bs` consecutive working rows: centre = normalised f64 sum (row order),
+// radius = the largest angle between a row and the centre (f64). Rows past n are ignored.
+__global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const uint32_t* __restrict__ perm, int n,
+                             int bs, double* __restrict__ center, double* __restrict__ radius) {
+    __shared__ double c_s[64];
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    const int r0 = b * bs, r1 = min(n, r0 + bs);
+    if (threadIdx.x < d) {
+        double s = 0.0;
+        for (int w = r0; w < r1; ++w) s += (double)xsT[(size_t)threadIdx.x * np + perm[w]];
+        c_s[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double nn = 0.0;
+        for (int t = 0; t < d; ++t) nn += c_s[t] * c_s[t];
+        const double inv = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+        for (int t = 0; t < d; ++t) c_s[t] *= inv;
+    }
+    __syncthreads();
+    if (threadIdx.x < d) center[(size_t)b * d + threadIdx.x] = c_s[threadIdx.x];
+    double worst = 0.0;
+    for (int w = r0 + threadIdx.x; w < r1; w += blockDim.x) {
+        const uint32_t o = perm[w];
+        double dot = 0.0, nn = 0.0;
+        for (int t = 0; t < d; ++t) {
+            const double v = (double)xsT[(size_t)t * np + o];
+            dot += v * c_s[t];
+            nn += v * v;
+        }
+        // zero rows have cosine 0 with everything: angle π/2 covers them
+        const double cs = nn > 0.0 ? dot / sqrt(nn) : 0.0;
+        worst = fmax(worst, acos(fmin(1.0, fmax(-1.0, cs))));
+    }
+    red[threadIdx.x] = worst;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) radius[b] = red[0];
+}
+
+// ---- per-query-block lists ------------------------------------------------------------------------
+
+constexpr int LIST_T = 512;
+constexpr double XI = 1e-6;
+
+__device__ __forceinline__ double block_ub(const double* cq, double rq, const double* cb, double rb, int d) {
+    double dot = 0.0;
+    for (int t = 0; t < d; ++t) dot += cq[t] * cb[t];
+    const double phi = acos(fmin(1.0, fmax(-1.0, dot)));
+    const double th = fmax(0.0, phi - rq - rb - XI);
+    return cos(th);
+}
+
+// One CTA per query block: the upper bound against every column block, the blocks kept (UB ≥ t_Q)
+// sorted by UB descending (shared-memory bitonic sort when they fit, else in block order), and the
+// largest UB of a skipped block.
+__global__ void __launch_bounds__(LIST_T)
+    k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
+                  const double* __restrict__ ccenter, const double* __restrict__ cradius, int nqb, int ncb, int d,
+                  const float* __restrict__ tq, uint32_t* __restrict__ lists, uint32_t* __restrict__ counts,
+                  float* __restrict__ ub_skip, unsigned long long* __restrict__ skipped_total) {
+    extern __shared__ unsigned char sm[];
+    float* key = reinterpret_cast<float*>(sm);              // [8192]
+    uint32_t* id = reinterpret_cast<uint32_t*>(key + 8192);  // [8192]
+    __shared__ double cq[64];
+    __shared__ unsigned kept;
+    __shared__ int skip_max_bits;
+    const int Q = blockIdx.x;
+    if (threadIdx.x < d) cq[threadIdx.x] = qcenter[(size_t)Q * d + threadIdx.x];
+    if (threadIdx.x == 0) {
+        kept = 0;
+        skip_max_bits = __float_as_int(-CUDART_INF_F);
+    }
+    __syncthreads();
+    const double rq = qradius[Q];
+    const float t = tq ? tq[Q] : -CUDART_INF_F;
+    const bool sortable = ncb <= 8192;
+    uint32_t* out = lists + (size_t)Q * ncb;
+    for (int b = threadIdx.x; b < ncb; b += blockDim.x) {
+        const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
+        float ubf = (float)ub;
+        if ((double)ubf < ub) ubf = nextafterf(ubf, CUDART_INF_F);  // round the bound up
+        const bool keep = ubf >= t;
+        if (keep) atomicAdd(&kept, 1u);
+        // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
+        else atomicMax(&skip_max_bits, __float_as_int(fmaxf(ubf, 0.0f)));
+        if (sortable) {
+            key[b] = keep ? ubf : -CUDART_INF_F;
+            id[b] = keep ? (uint32_t)b : 0xffffffffu;
+        }
+    }
+    __syncthreads();
+    if (sortable) {
+        int np2 = 1;
+        while (np2 < ncb) np2 <<= 1;
+        for (int b = ncb + threadIdx.x; b < np2; b += blockDim.x) {
+            key[b] = -CUDART_INF_F;
+            id[b] = 0xffffffffu;
+        }
+        __syncthreads();
+        // bitonic sort into (bound desc, block id asc); dropped blocks (−∞, id max) go last
+        for (int size = 2; size <= np2; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int e = threadIdx.x; e < np2 / 2; e += blockDim.x) {
+                    const int lo = 2 * e - (e & (stride - 1)), hi = lo + stride;
+                    const bool hi_before = key[hi] > key[lo] || (key[hi] == key[lo] && id[hi] < id[lo]);
+                    const bool lo_before = key[lo] > key[hi] || (key[lo] == key[hi] && id[lo] < id[hi]);
+                    if ((lo & size) == 0 ? hi_before : lo_before) {
+                        const float a = key[lo];
+                        key[lo] = key[hi];
+                        key[hi] = a;
+                        const uint32_t c = id[lo];
+                        id[lo] = id[hi];
+                        id[hi] = c;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (unsigned b = threadIdx.x; b < kept; b += blockDim.x) out[b] = id[b];
+    } else if (threadIdx.x == 0) {
+        unsigned c = 0;
+        for (int b = 0; b < ncb; ++b) {
+            const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
+            float ubf = (float)ub;
+            if ((double)ubf < ub) ubf = nextafterf(ubf, CUDART_INF_F);
+            if (ubf >= t) out[c++] = (uint32_t)b;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        counts[Q] = kept;
+        ub_skip[Q] = __int_as_float(skip_max_bits);
+        if (skipped_total) atomicAdd(skipped_total, (unsigned long long)(ncb - (int)kept));
+    }
+}
+
+// The per-row certificate floor from pruning: ub_skip of the row's query block, or −∞.
+__global__ void k_row_ub(const uint32_t* __restrict__ perm, int n, const float* __restrict__ ub_skip,
+                         double* __restrict__ row_ub) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n) return;
+    const float u = ub_skip[w / 128];
+    row_ub[perm[w]] = u == -CUDART_INF_F ? -CUDART_INF : (double)u;
+}
+
+}  // namespace prune
+}  // namespace costal
+
+namespace costal {
+namespace prune {
+
+namespace {
+inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+}  // namespace
+
+bool supported(int d) { return d >= 1 && d <= 64; }
+
+size_t workspace_bytes(int n, int d) {
+    const size_t nqb = (size_t)(n + QB - 1) / QB, ncb = (size_t)(n + CB - 1) / CB;
+    const size_t m = (size_t)(n < SAMPLE ? n : SAMPLE), nch = (size_t)(n + CHUNK - 1) / CHUNK;
+    return a256(n * 4ull) * 2 + a256((size_t)K_CENTROIDS * d * 4) + a256(nqb * d * 8) + a256(nqb * 8) +
+           a256(ncb * d * 8) + a256(ncb * 8) + a256(nqb * ncb * 4) + a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) +
+           a256(nqb * 4) + a256(m * d * 4) + a256(m * 4) + a256(nch * K_CENTROIDS * 4) + a256((K_CENTROIDS + 1) * 4) +
+           a256(m * 4) + 4096;
+}
+
+namespace {
+struct Scratch {
+    float* sample_rows;
+    uint32_t* sample_assign;
+    uint32_t* hist;
+    uint32_t* cell_start;
+    uint32_t* sample_idx;
+};
+
+__global__ void k_sample_idx(uint32_t* idx, int m, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) idx[j] = (uint32_t)(((unsigned long long)j * (unsigned long long)n) / (unsigned long long)m);
+}
+
+// Initial centroids: K evenly spaced sample rows (deterministic).
+__global__ void k_init_centroids(const float* rows, int m, int d, int K, float* cent) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= K * d) return;
+    const int c = e / d, t = e % d;
+    const int i = (int)(((long long)c * m) / K);
+    cent[e] = rows[(size_t)i * d + t];
+}
+}  // namespace
+
+cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaStream_t st, Plan& P) {
+    const int K = K_CENTROIDS;
+    const int nqb = (n + QB - 1) / QB, ncb = (n + CB - 1) / CB;
+    const int m = n < SAMPLE ? n : SAMPLE, nch = (n + CHUNK - 1) / CHUNK;
+    char* p = static_cast<char*>(ws);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += a256(bytes);
+        return r;
+    };
+    P.n = n;
+    P.d = d;
+    P.K = K;
+    P.nqb = nqb;
+    P.ncb = ncb;
+    P.perm = reinterpret_cast<uint32_t*>(take(n * 4ull));
+    P.cell = reinterpret_cast<uint32_t*>(take(n * 4ull));
+    P.centroids = reinterpret_cast<float*>(take((size_t)K * d * 4));
+    P.qcenter = reinterpret_cast<double*>(take((size_t)nqb * d * 8));
+    P.qradius = reinterpret_cast<double*>(take((size_t)nqb * 8));
+    P.ccenter = reinterpret_cast<double*>(take((size_t)ncb * d * 8));
+    P.cradius = reinterpret_cast<double*>(take((size_t)ncb * 8));
+    P.lists = reinterpret_cast<uint32_t*>(take((size_t)nqb * ncb * 4));
+    P.counts = reinterpret_cast<uint32_t*>(take((size_t)nqb * 4));
+    P.ub_skip = reinterpret_cast<float*>(take((size_t)nqb * 4));
+    P.row_ub = reinterpret_cast<double*>(take(n * 8ull));
+    P.tq = reinterpret_cast<float*>(take((size_t)nqb * 4));
+    Scratch S;
+    S.sample_rows = reinterpret_cast<float*>(take((size_t)m * d * 4));
+    S.sample_assign = reinterpret_cast<uint32_t*>(take((size_t)m * 4));
+    S.hist = reinterpret_cast<uint32_t*>(take((size_t)nch * K * 4));
+    S.cell_start = reinterpret_cast<uint32_t*>(take((size_t)(K + 1) * 4));
+    S.sample_idx = reinterpret_cast<uint32_t*>(take((size_t)m * 4));
+    P.scratch = S.sample_rows;
+
+    const size_t csm = (size_t)K * d * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_assign, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
+    if (e != cudaSuccess) return e;
+    k_sample_idx<<<(m + 255) / 256, 256, 0, st>>>(S.sample_idx, m, n);
+    k_gather_rows<<<1024, 256, 0, st>>>(xsT, np, d, S.sample_idx, m, S.sample_rows);
+    k_init_centroids<<<(K * d + 255) / 256, 256, 0, st>>>(S.sample_rows, m, d, K, P.centroids);
+    for (int it = 0; it < LLOYD_STEPS; ++it) {
+        k_assign<<<(m + KM_BLOCK - 1) / KM_BLOCK, KM_BLOCK, csm, st>>>(S.sample_rows, nullptr, np, m, d, P.centroids, K,
+                                                                         S.sample_assign);
+        k_centroid_update<<<K, UPD_T, 0, st>>>(S.sample_rows, m, d, S.sample_assign, P.centroids);
+    }
+    k_assign<<<(n + KM_BLOCK - 1) / KM_BLOCK, KM_BLOCK, csm, st>>>(nullptr, xsT, np, n, d, P.centroids, K, P.cell);
+    k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist);
+    k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start);
+    k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm);
+    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius);
+    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius);
+    return cudaGetLastError();
+}
+
+cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t st) {
+    const size_t smem = 8192 * 8;
+    cudaError_t e = cudaFuncSetAttribute(k_block_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_block_lists<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter, P.cradius, P.nqb, P.ncb, P.d, P.tq,
+                                              P.lists, P.counts, P.ub_skip, skipped_total);
+    k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub);
+    return cudaGetLastError();
+}
+
+}  // namespace prune
+}  // namespace costal

@@ -66,6 +66,7 @@ typedef struct costal_knn_stats {
     uint64_t pruned_fallback_rows; /* learned pruning: rows whose skip was not certified, rescanned */
     double max_coarse_err;     /* max |coarse score - f64 rescored score| over all kept candidates */
     double ms_prep, ms_coarse, ms_rescore, ms_fallback, ms_total; /* CUDA-event times of the stages */
+    double ms_order;           /* bf16 backend: locality order, block bounds and lists (inside ms_total) */
 } costal_knn_stats;
 
 /* ---- module surface (crates/costal-py/src/lib.rs:80-102, 430-446) ---------------------------- */
@@ -113,6 +114,47 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
  * capture). All calls share the array: calls that overlap on the GPU race and must be serialised. */
 int costal_reweight_jaccard_device_noalloc(const int32_t* d_idx, uint64_t n, uint32_t k, double* d_out, void* stream,
                                            char* err, size_t errlen);
+
+/* ---- the learned block-pruning model (GB300 addition; no counterpart in the reference) -------------
+ * An MLP (d + 64 centroid cosines -> 128 -> 128 -> 1) predicts each row's k-th-neighbour cosine; with
+ * costal_knn_opts.learned_prune = 1 and the bf16 backend, column blocks whose rigorous upper bound is
+ * below a query block's smallest prediction are skipped, and every skip is certified afterwards (a row
+ * whose k-th score does not beat its skipped blocks' bound is rescanned in full). */
+typedef struct costal_mlp_opts {
+    uint32_t sample;    /* rows used for training (evenly spaced); 0 = all rows; default 200,000 */
+    uint32_t epochs;    /* passes over the sample (default 30) */
+    uint32_t batch;     /* rows per Adam step (default 2048) */
+    uint32_t margin;    /* over-selection of the FP32 label pass; UINT32_MAX = k */
+    float lr;           /* Adam learning rate (default 2e-3) */
+    float quantile;     /* pinball-loss quantile (default 0.05: predictions below the truth for ~95% of rows) */
+    uint64_t seed;      /* parameter initialisation */
+} costal_mlp_opts;
+
+typedef struct costal_mlp_stats {
+    uint64_t samples, steps, params;
+    double loss;        /* final mean pinball loss on the training rows (bf16 weights) */
+    double mae;         /* mean |prediction - exact k-th cosine| */
+    double coverage;    /* fraction of training rows whose prediction is <= their exact k-th cosine */
+    double ms_labels;   /* exact labels (plain FP32 path) and features */
+    double ms_train;    /* forward/backward/Adam kernels */
+} costal_mlp_stats;
+
+/* Train the model on X (host, n x d): labels are the exact k-th-neighbour cosines of the sampled rows
+ * from the plain FP32 path, features use the same k-means cells as the pruned kNN. The model stays
+ * loaded in the library's context. mo may be NULL (defaults). */
+int costal_mlp_train(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_mlp_opts* mo,
+                     costal_mlp_stats* stats, char* err, size_t errlen);
+/* Checkpointing: read (params may be NULL to query *count) or load the f32 master weights. */
+int costal_mlp_get(float* params, uint64_t capacity, uint64_t* count, uint32_t* d, uint32_t* k, float* quantile,
+                   char* err, size_t errlen);
+int costal_mlp_set(const float* params, uint64_t count, uint32_t d, uint32_t k, float quantile, char* err,
+                   size_t errlen);
+int costal_mlp_clear(char* err, size_t errlen);
+/* Test hooks: the forward pass and the loss gradient for given weights and features (host buffers). */
+int costal_mlp_forward(const float* params, uint32_t F, const float* feat, uint64_t m, float* out, char* err,
+                       size_t errlen);
+int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, const float* y, uint64_t m,
+                        float quantile, float* grad, char* err, size_t errlen);
 
 /* ---- the host consumer: Leiden (leiden="fast"), crates/costal-core/src/leiden.rs ------------- */
 /* lib.rs:275-306 `_leiden` (from_coo = 0, objective = 0) and lib.rs:356-412 `_leiden_coo`

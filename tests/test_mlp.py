@@ -1,0 +1,74 @@
+"""The learned block-pruning model: GPU forward/backward against the numpy restatement, training,
+exactness of the pruned kNN, and what the trained network gains over the method without it."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_forward_and_gradient_match_the_oracle(ext):
+    from oracle import mlp_oracle as M
+
+    rng = np.random.default_rng(0)
+    for F, m in ((30, 100), (104, 257)):
+        params = (rng.standard_normal(M.param_count(F)) * 0.15).astype(np.float32)
+        feat = rng.standard_normal((m, F)).astype(np.float32)
+        y = rng.standard_normal(m).astype(np.float32)
+        out = ext._mlp_forward(params, feat)
+        want, _ = M.forward(params, feat)
+        np.testing.assert_allclose(out, want, rtol=1e-4, atol=1e-4)
+        g = ext._mlp_gradient(params, feat, y, 0.05).astype(np.float64)
+        gw = M.gradient(params, feat, y, 0.05)
+        assert np.linalg.norm(g - gw) <= 1e-4 * np.linalg.norm(gw)
+
+
+@pytest.fixture(scope="module")
+def zipf_case(ext):
+    from costal_gb300 import workloads as W
+
+    x, wl = W.make("zipf_2m", n=60_000)
+    ref = ext._knn_exact(x, wl.k, margin=wl.margin)[0]
+    stats = ext._mlp_train(x, wl.k, sample=60_000, epochs=30, batch=1024)
+    return x, wl, ref, stats
+
+
+def test_training_is_conservative(zipf_case):
+    _, _, _, stats = zipf_case
+    assert stats["samples"] == 60_000 and stats["steps"] > 0
+    assert stats["coverage"] > 0.85  # pinball loss at the 5% quantile: predictions mostly below
+    assert stats["mae"] < 0.25
+
+
+def test_learned_pruning_is_exact_and_skips_blocks(ext, zipf_case):
+    x, wl, ref, _ = zipf_case
+    got, st = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
+    assert st["blocks_skipped"] > 0.1 * st["blocks_total"], st
+    unpruned, st0 = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16")
+    assert st0["blocks_skipped"] == 0
+    for a, b in zip(unpruned, ref):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_trained_network_beats_a_constant_threshold(ext, zipf_case):
+    """Ablation: the same pruning with a constant predictor (the 5% quantile of the exact k-th
+    cosines, i.e. the best one number for the same coverage) skips fewer blocks."""
+    from oracle import mlp_oracle as M
+
+    x, wl, ref, _ = zipf_case
+    params, d, k, q = ext._mlp_get()
+    _, st_mlp = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+    const = np.zeros(M.param_count(d + 64), np.float32)
+    const[-1] = np.quantile(ref[1][:, wl.k - 1], 0.05)
+    ext._mlp_set(const, d, k, q)
+    try:
+        got, st_c = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+        for a, b in zip(got, ref):
+            np.testing.assert_array_equal(a, b)
+    finally:
+        ext._mlp_set(params, d, k, q)  # restore the trained model (checkpoint round trip)
+    assert st_mlp["blocks_skipped"] > st_c["blocks_skipped"], (st_mlp, st_c)
+    _, st_back = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+    assert st_back["blocks_skipped"] == st_mlp["blocks_skipped"]
