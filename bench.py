@@ -1,17 +1,25 @@
 """Benchmark: exact kNN-graph cells/s on one GB300 (one JSON line on stdout).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--backend fp32|bf16]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--backend bf16|fp32]
     python bench.py --impl reference ...      # the CPU implementation of the path on the host cores
 
+Default workload: 2,000,000 × 40 f32, 50 clusters with Zipf(1.2) sizes, arcsinh(x/5), k = 10, m = 10
+(the learned-prune configuration), certified split-BF16 tensor-core coarse pass with learned block
+pruning, against the plain FP32 GPU path on the same input.
+
 A step is one pass of the hot path over one batch: X (n × d f32) -> norms, normalised tiles, top-(k+m)
-selection, f64 rescoring + certificate (+ regather), Tanimoto weights, fuzzy-union edge list.
+selection, f64 rescoring + certificate (+ recomputation / regather), Tanimoto weights, fuzzy-union
+edge list. With the learned backend the step also includes the k-means locality order, the model's
+inference and the block lists; the model itself is trained once before timing (reported as `train`).
 
   value  — n / step time with X already resident in HBM (CUDA events on the launching stream, L2
            flushed between steps by writing a 512 MB buffer outside the timed events);
   e2e    — the same through the host C-ABI call costal_build_graph: pinned host X in, pinned host
            edge list out, copies inside the timed region (wall clock around the synchronous call);
-  roofline — the dominant kernel (the coarse tile + selection kernel), achieved algorithmic FLOP/s
-           (2·n·(n−1)·d per launch, dense-equivalent) over its CUDA-event duration;
+  plain_fp32 — the plain FP32 GPU path on the same input (device-resident, same timing);
+  roofline — the dominant kernel (the coarse tile + selection kernel): algorithmic FLOP/s (2·d per
+           visited pair: pairs of the tiles neither skipped by the learned threshold nor left out by
+           the exact early stop) over its CUDA-event duration;
   cpu_baseline — the oracle (C++ restatement of the reference's CPU path) on a bounded sample of
            query rows, all host threads.
 
@@ -102,6 +110,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def traffic_per_launch(backend, pairs):
+    """DRAM bytes (read + write) per launch of the dominant kernel: bytes per visited pair from the
+    committed ncu capture summary profiles/dram_traffic.json, times this launch's visited pairs.
+    None when no capture exists for the backend."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    rec = json.loads(p.read_text()).get(backend)
+    if not rec:
+        return None
+    return rec["bytes_per_pair"] * pairs
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -161,9 +182,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rare_400k")
+    ap.add_argument("--workload", default="zipf_2m")
     ap.add_argument("--n", type=int, default=None, help="a smaller n from the same generator (profiling)")
-    ap.add_argument("--backend", default="fp32", choices=["fp32", "bf16"])
+    ap.add_argument("--backend", default="bf16", choices=["fp32", "bf16"])
+    ap.add_argument("--no-learned", action="store_true", help="bf16 backend without the learned pruning")
+    ap.add_argument("--train-sample", type=int, default=200_000)
+    ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP32 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
@@ -192,14 +217,36 @@ def main():
 
     lib = L.lib()
     n, d, k = wl.n, wl.d, wl.k
-    opts = L.KnnOpts()
-    opts.margin = wl.margin
-    opts.select = 0
-    opts.backend = L.BACKEND_BF16 if args.backend == "bf16" else L.BACKEND_FP32
-    opts.sort_by_norm = 1
-    opts.prune = 1
+    learned = args.backend == "bf16" and not args.no_learned
+    err, errlen = L.errbuf()
+
+    def make_opts(backend, learned_prune):
+        o = L.KnnOpts()
+        o.margin = wl.margin
+        o.select = 0
+        o.backend = L.BACKEND_BF16 if backend == "bf16" else L.BACKEND_FP32
+        o.sort_by_norm = 1
+        o.prune = 1
+        o.learned_prune = 1 if learned_prune else 0
+        return o
+
+    opts = make_opts(args.backend, learned)
     weight = L.WEIGHT["tanimoto"]
     stream = torch.cuda.current_stream()
+
+    # ---- the model (trained once on this input, labels from the plain FP32 path; untimed)
+    train = None
+    if learned:
+        mo = L.MlpOpts()
+        mo.sample, mo.epochs, mo.batch = min(args.train_sample, n), args.train_epochs, 2048
+        mo.margin, mo.lr, mo.quantile, mo.seed = wl.margin, 2e-3, 0.05, 20241203
+        ms_ = L.MlpStats()
+        t = time.perf_counter()
+        L.check(lib.costal_mlp_train(x.ctypes.data_as(C.c_void_p), n, d, k, C.byref(mo), C.byref(ms_), err, errlen),
+                err)
+        train = {kk: v for kk, v in ms_.as_dict().items()}
+        train["wall_s"] = time.perf_counter() - t
+
     dx = torch.from_numpy(x).cuda()
     d_rows = torch.empty(n * k, dtype=torch.int32, device="cuda")
     d_cols = torch.empty(n * k, dtype=torch.int32, device="cuda")
@@ -207,44 +254,47 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     m = C.c_uint64()
     st = L.KnnStats()
-    err, errlen = L.errbuf()
 
-    def step_device():
-        rc = lib.costal_build_graph_device(C.c_void_p(dx.data_ptr()), n, d, k, C.byref(opts), weight,
+    def step_device(o):
+        rc = lib.costal_build_graph_device(C.c_void_p(dx.data_ptr()), n, d, k, C.byref(o), weight,
                                            C.c_void_p(d_rows.data_ptr()), C.c_void_p(d_cols.data_ptr()),
                                            C.c_void_p(d_w.data_ptr()), C.byref(m), C.byref(st),
                                            C.c_void_p(stream.cuda_stream), err, errlen)
         L.check(rc, err)
 
-    # ---- device-resident value
-    for _ in range(args.warmup):
-        flush.zero_()
-        step_device()
-    torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    times, coarse_ms, stats = [], [], []
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
+    def timed_device(o, warmup, steps, clocks=None):
+        for _ in range(warmup):
+            flush.zero_()
+            step_device(o)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        times, stats = [], []
+        l0 = lib.costal_launch_count()
+        for _ in range(steps):
             flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            step_device()
+            step_device(o)
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            coarse_ms.append(st.ms_coarse)
             stats.append(st.as_dict())
-    torch.cuda.synchronize()
-    ms = float(np.mean(times))
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    edges = int(m.value)
+        launches = lib.costal_launch_count() - l0
+        torch.cuda.synchronize()
+        ms = float(np.mean(times))
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms, stats, launches, int(m.value)
+
+    # ---- device-resident value
+    with ClockSampler(local) as clocks:
+        ms, stats, launches, edges = timed_device(opts, args.warmup, args.steps)
 
     # ---- end to end through the host C ABI (pinned host buffers, copies inside the timed region)
     hx = torch.from_numpy(x).pin_memory()
@@ -277,20 +327,44 @@ def main():
         e2e_s = float(t.item())
     # parity guard: the timed host result equals the device-resident one
     assert int(m2.value) == edges
+    host_edges = (h_rows[:edges].numpy().copy(), h_cols[:edges].numpy().copy(), h_w[:edges].numpy().copy())
+
+    # ---- the plain FP32 GPU path on the same input (the comparison the metric names)
+    plain = None
+    if args.backend == "bf16" and args.plain_steps > 0:
+        pms, pstats, _, pedges = timed_device(make_opts("fp32", False), 1, args.plain_steps)
+        same = pedges == edges and all(
+            np.array_equal(a, b.cpu().numpy()[:edges]) for a, b in zip(host_edges, (d_rows, d_cols, d_w)))
+        plain = {"ms_per_step": pms, "value": ws * n / (pms * 1e-3), "unit": "cells/s", "steps": args.plain_steps,
+                 "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in pstats])),
+                 "speedup": pms / ms, "identical_edges": bool(same)}
 
     if rank == 0:
         pk, pk_kind = peaks()
-        cm = float(np.mean(coarse_ms))
-        flops = 2.0 * n * (n - 1) * d
         s0 = stats[-1]
+        kms = float(np.mean([s_["ms_kernel"] for s_ in stats]))
+        total_blocks = s0["blocks_total"]
+        skipped = s0["blocks_skipped"] + s0["blocks_stopped"] if args.backend == "bf16" else 0
+        visited = 1.0 - skipped / total_blocks if total_blocks else 1.0
+        pairs = float(n) * float(n) * visited  # dense pairs of the visited (query block, column block) tiles
+        flops = 2.0 * d * pairs
         if args.backend == "bf16":
-            bound, peak, unit = "tensor", pk["bf16_tflops"], "TFLOP/s"
+            kpad = (3 * d + 63) // 64 * 64
+            tiles = (total_blocks - skipped)
+            executed = 2.0 * kpad * tiles * 128 * 256
+            bound, peak, unit = "tensor", pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s"
+            kernel = "k_coarse_tc (split-BF16 tcgen05 tiles + top-(k+m) selection)"
+            peak_kind = f"bf16 dense sustained, {pk_kind}"
         else:
+            executed = flops
             # FP32 FFMA peak of the GB300 (152 SMs x 128 lanes x 2 FLOP x max SM clock); MEASURED_PEAKS
             # has no CUDA-core figure, so it is derived from the measured max clock.
             bound, unit = "fp32-fma", "TFLOP/s"
             peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-        achieved = flops / (cm * 1e-3) / 1e12
+            kernel = "k_coarse_fp32 (FP32 tiles + top-(k+m) selection)"
+            peak_kind = "derived FP32-FFMA peak at max SM clock"
+        achieved = flops / (kms * 1e-3) / 1e12
+        traffic = traffic_per_launch(args.backend, pairs)
         line = {
             "metric": METRIC,
             "value": ws * n / (ms * 1e-3),
@@ -302,23 +376,33 @@ def main():
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 tiles + f64 rescoring" if args.backend == "fp32" else "split-bf16 tcgen05 tiles + f64 rescoring",
+            "dtype": ("split-bf16 tcgen05 tiles (fp32 accumulate) + f64 rescoring" if args.backend == "bf16"
+                      else "f32 tiles + f64 rescoring"),
             "data": "synthetic (seeded generator with the workload's shapes and distributions)",
             "config": {"workload": wl.name, "n": n, "d": d, "k": k, "margin": wl.margin, "backend": args.backend,
-                       "weight": "tanimoto", "l2": "flushed between steps (512 MB write outside the timed events)"},
+                       "learned_prune": learned, "weight": "tanimoto",
+                       "l2": "flushed between steps (512 MB write outside the timed events)"},
             "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
                     "d2h_bytes_per_step": edges * 16},
-            "gpu_launches": None,
+            "gpu_launches": int(launches),
+            "gpu_launches_per_step": launches / args.steps,
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-                         "traffic": None, "kernel": "coarse tile + top-(k+m) selection",
-                         "peak_kind": ("derived FP32-FFMA peak at max SM clock" if args.backend == "fp32"
-                                       else f"bf16 dense, {pk_kind}")},
-            "pair_dots_per_s": ws * n * (n - 1) / (ms * 1e-3),
+                         "traffic": traffic, "kernel": kernel, "peak_kind": peak_kind,
+                         "ms_per_launch": kms, "pairs_per_launch": pairs,
+                         "executed_tflops": executed / (kms * 1e-3) / 1e12,
+                         "executed_frac": executed / (kms * 1e-3) / 1e12 / peak},
+            "pair_dots_per_s": ws * float(n) * (n - 1) / (ms * 1e-3),
             "edges": edges,
-            "stats": {kk: s0[kk] for kk in ("fallback_rows", "recomputed_rows", "max_coarse_err", "ms_prep",
-                                             "ms_coarse", "ms_rescore", "ms_fallback", "ms_total")},
+            "plain_fp32": plain,
+            "train": train,
+            "stats": {kk: s0[kk] for kk in ("fallback_rows", "recomputed_rows", "pruned_fallback_rows",
+                                             "blocks_skipped", "blocks_stopped", "blocks_total", "max_coarse_err", "ms_prep",
+                                             "ms_order", "ms_coarse", "ms_kernel", "ms_rescore", "ms_fallback",
+                                             "ms_total")},
             "clocks": clocks.summary(),
         }
+        if train is not None:
+            line["value_incl_training"] = ws * n / ((ms + train["ms_labels"] + train["ms_train"]) * 1e-3)
         if not args.no_cpu:
             v, cores, sample = cpu_baseline(x, wl, target_s=args.cpu_seconds)
             line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample}

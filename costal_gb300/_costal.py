@@ -2,7 +2,7 @@
 
 Same functions, signatures, return types and error behaviour as the PyO3 module of
 crates/costal-py/src/lib.rs:80-465; the reference's pure-Python package (`costal._api`,
-`costal._leiden`) runs unchanged on top of it (INTEGRATION.md shows how to install it). Only type
+`costal._leiden`) runs unchanged on top of it. Only type
 conversion and error mapping live here — as in lib.rs — and every computation is a call into
 libcostal_gb300.so: the kNN graph on the GPU, Leiden (the host consumer) in host C++.
 
@@ -11,8 +11,9 @@ Differences from the reference, all documented:
     its alias) or "bf16" (certified split-BF16 tcgen05 tiles). Like the reference's backends they
     change speed only, never the output. "accelerate" is Apple-only and unavailable here, as it is
     for the reference on Linux.
-  - `row_block`, `col_block`, `sort_by_norm`, `prune` and `n_threads` are accepted and validated
-    but do not change the GPU tiling (the reference: they change speed only, knn.rs:39-44).
+  - `row_block`, `col_block`, `sort_by_norm` and `n_threads` are accepted and validated but do not
+    change the GPU tiling (the reference: they change speed only, knn.rs:39-44). `prune` (speed
+    only, as in the reference) switches the exact early stop of the bf16 backend's block lists.
   - k + margin above 128 raises NotImplementedError (the GPU keeps at most 128 candidates a row).
 """
 
@@ -139,6 +140,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
         "recomputed_rows": int(st.recomputed_rows),
         "pruned_fallback_rows": int(st.pruned_fallback_rows),
         "max_coarse_err": float(st.max_coarse_err),
+        "blocks_stopped": int(st.blocks_stopped),
         "ms_order": float(st.ms_order),
         "ms_coarse": float(st.ms_coarse),
         "ms_total": float(st.ms_total),

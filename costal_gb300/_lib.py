@@ -55,6 +55,8 @@ class KnnStats(C.Structure):
         ("ms_fallback", C.c_double),
         ("ms_total", C.c_double),
         ("ms_order", C.c_double),
+        ("ms_kernel", C.c_double),
+        ("blocks_stopped", C.c_uint64),
     ]
 
     def as_dict(self):
@@ -134,6 +136,8 @@ def lib() -> C.CDLL:
             fn.restype = C.c_int
         lb.costal_version.argtypes = []
         lb.costal_version.restype = C.c_char_p
+        lb.costal_launch_count.argtypes = []
+        lb.costal_launch_count.restype = C.c_ulonglong
         _lib = lb
     return _lib
 

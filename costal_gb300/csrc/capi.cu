@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,6 +18,14 @@
 #include "knn_tc.h"
 #include "mlp.h"
 #include "prune.h"
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}  // namespace
+
+namespace costal {
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace costal
 
 namespace {
 
@@ -41,6 +50,7 @@ struct Misc {  // small device-side results read back at the end of a call
     unsigned prune_fail_count;
     unsigned long long blocks_skipped;
     unsigned long long timeout_flag;
+    unsigned long long blocks_stopped;
 };
 
 struct Context {
@@ -221,8 +231,10 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
             CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, pp.perm, s, plan));
-            CK(tc::launch_coarse(plan, cap, pp.lists, pp.counts, pp.ncb, c.cand_idx.as<uint32_t>(),
-                                 c.cand_score.as<float>(), c.tau.as<float>(), &dm->timeout_flag, c.sm_count, s));
+            CK(cudaEventRecord(c.ev[6], s));
+            CK(tc::launch_coarse(plan, cap, pp.lists, o.prune ? pp.list_ub : nullptr, pp.counts, pp.ncb, c.cand_idx.as<uint32_t>(),
+                                 c.cand_score.as<float>(), c.tau.as<float>(), &dm->blocks_stopped, &dm->timeout_flag,
+                                 c.sm_count, s));
             CK(cudaEventRecord(c.ev[2], s));
             // The split-BF16 certificate with its per-row bound (and, with pruning, the skipped
             // blocks' bound); rows that fail it are listed in tc_rows, re-run over ALL columns by the
@@ -275,6 +287,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         st->row_block = 128;
         st->col_block = used_tc ? (uint64_t)tc::BLOCK_N : 128;
         st->blocks_skipped = hm.blocks_skipped;
+        st->blocks_stopped = hm.blocks_stopped;
         st->blocks_total = (uint64_t)((n + 127) / 128) * (uint64_t)((n + st->col_block - 1) / st->col_block);
         st->margin = margin;
         st->recomputed_rows = used_tc ? hm.tc_fail_count : 0;
@@ -288,6 +301,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         st->ms_rescore = elapsed(c.ev[2], c.ev[3]);
         st->ms_fallback = elapsed(c.ev[3], c.ev[4]);
         st->ms_total = elapsed(c.ev[0], c.ev[4]);
+        st->ms_kernel = used_tc ? elapsed(c.ev[6], c.ev[2]) : st->ms_coarse;
     }
 }
 
@@ -350,6 +364,8 @@ void check_neighbours(Context& c, const int32_t* d_idx, const int32_t* h_idx, ui
 extern "C" {
 
 const char* costal_version(void) { return "2.1.0"; }
+
+unsigned long long costal_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int costal_device_ok(char* err, size_t errlen) {
     return guarded(err, errlen, [](Context&) {});

@@ -272,7 +272,7 @@ cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lst
     cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_coarse_fp32<S, D><<<np / BM, NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score,
-                                                   tau);
+                                                   tau); note_launch();
     return cudaGetLastError();
 }
 

@@ -8,6 +8,10 @@
 
 namespace costal {
 
+// Counts every kernel launch this library issues (host side, relaxed atomic); read through
+// costal_launch_count().
+void note_launch();
+
 // ---- exact f64 arithmetic in the reference's order of operations ---------------------------------
 //
 // Each helper names the rounding of every operation, so nvcc can never contract a multiply and an

@@ -31,7 +31,7 @@ __global__ void k_check_idx(const int32_t* __restrict__ idx, uint64_t nk, int n,
 
 cudaError_t launch_check_idx(const int32_t* idx, uint64_t nk, int n, unsigned long long* first_bad, cudaStream_t st) {
     if (nk == 0) return cudaSuccess;
-    k_check_idx<<<1024, 256, 0, st>>>(idx, nk, n, first_bad);
+    k_check_idx<<<1024, 256, 0, st>>>(idx, nk, n, first_bad); note_launch();
     return cudaGetLastError();
 }
 
@@ -41,7 +41,7 @@ __global__ void k_iota(uint32_t* __restrict__ out, int start, int m) {
     if (i < m) out[i] = (uint32_t)(start + i);
 }
 cudaError_t launch_iota(uint32_t* out, int start, int m, cudaStream_t st) {
-    if (m > 0) k_iota<<<(m + 255) / 256, 256, 0, st>>>(out, start, m);
+    if (m > 0) { k_iota<<<(m + 255) / 256, 256, 0, st>>>(out, start, m); note_launch(); }
     return cudaGetLastError();
 }
 // Evenly spaced sample rows: out[j] = ⌊j·n/m⌋.
@@ -50,7 +50,7 @@ __global__ void k_stride_rows(uint32_t* __restrict__ out, int m, int n) {
     if (j < m) out[j] = (uint32_t)(((unsigned long long)j * (unsigned long long)n) / (unsigned long long)m);
 }
 cudaError_t launch_stride_rows(uint32_t* out, int m, int n, cudaStream_t st) {
-    if (m > 0) k_stride_rows<<<(m + 255) / 256, 256, 0, st>>>(out, m, n);
+    if (m > 0) { k_stride_rows<<<(m + 255) / 256, 256, 0, st>>>(out, m, n); note_launch(); }
     return cudaGetLastError();
 }
 // y[j] = cos[rows[j]·k + k − 1]: the k-th neighbour cosine of each listed row.
@@ -60,7 +60,7 @@ __global__ void k_kth(const double* __restrict__ cos, const uint32_t* __restrict
     if (j < m) y[j] = (float)cos[(size_t)rows[j] * k + k - 1];
 }
 cudaError_t launch_kth(const double* cos, const uint32_t* rows, int m, int k, float* y, cudaStream_t st) {
-    if (m > 0) k_kth<<<(m + 255) / 256, 256, 0, st>>>(cos, rows, m, k, y);
+    if (m > 0) { k_kth<<<(m + 255) / 256, 256, 0, st>>>(cos, rows, m, k, y); note_launch(); }
     return cudaGetLastError();
 }
 // Deterministic He-uniform initialisation from a counter-based hash (SplitMix64 of seed + index).
@@ -81,7 +81,7 @@ __global__ void k_init_params(float* __restrict__ P, int F, unsigned long long s
     }
 }
 cudaError_t launch_init_params(float* P, int F, unsigned long long seed, cudaStream_t st) {
-    k_init_params<<<64, 256, 0, st>>>(P, F, seed);
+    k_init_params<<<64, 256, 0, st>>>(P, F, seed); note_launch();
     return cudaGetLastError();
 }
 
@@ -95,7 +95,7 @@ __global__ void k_tanimoto_w(const uint32_t* __restrict__ idx, const double* __r
 cudaError_t launch_tanimoto_w(const uint32_t* idx, const double* cos, const double* norms, uint64_t nk, int k,
                               double* out, cudaStream_t st) {
     if (nk == 0) return cudaSuccess;
-    k_tanimoto_w<<<2048, 256, 0, st>>>(idx, cos, norms, nk, k, out);
+    k_tanimoto_w<<<2048, 256, 0, st>>>(idx, cos, norms, nk, k, out); note_launch();
     return cudaGetLastError();
 }
 
@@ -134,8 +134,8 @@ __global__ void k_jaccard(const uint32_t* __restrict__ idx, const uint32_t* __re
 
 cudaError_t launch_jaccard(const uint32_t* idx, int n, int k, uint32_t* sorted_scratch, double* out, cudaStream_t st) {
     if (n == 0 || k == 0) return cudaSuccess;
-    k_sort_rows<<<(n + 127) / 128, 128, 0, st>>>(idx, n, k, sorted_scratch);
-    k_jaccard<<<2048, 256, 0, st>>>(idx, sorted_scratch, (uint64_t)n * k, k, out);
+    k_sort_rows<<<(n + 127) / 128, 128, 0, st>>>(idx, n, k, sorted_scratch); note_launch();
+    k_jaccard<<<2048, 256, 0, st>>>(idx, sorted_scratch, (uint64_t)n * k, k, out); note_launch();
     return cudaGetLastError();
 }
 
@@ -458,15 +458,15 @@ cudaError_t launch_fuzzy_union(const uint32_t* idx, const double* w, int n, int 
     if ((e = cudaMemsetAsync(s.cnt, 0, (n + 1) * 4ull, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(s.cursor, 0, n * 4ull, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(s.nbig, 0, 4, st)) != cudaSuccess) return e;
-    k_emit<<<2048, 256, 0, st>>>(idx, w, n, k, s);
+    k_emit<<<2048, 256, 0, st>>>(idx, w, n, k, s); note_launch();
     const int len = n + 1;
     const int nb = (len + SCAN_B - 1) / SCAN_B;
-    k_scan_blocks<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum);
-    k_scan_sums<<<1, SCAN_B, 0, st>>>(s.bsum, nb, m_dev);
-    k_scan_add<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum);
-    k_scatter<<<2048, 256, 0, st>>>(n, k, s);
-    k_sort_small<<<(n + 7) / 8, 256, 0, st>>>(n, s, rows, cols, w_out);
-    k_sort_big<<<256, 512, 0, st>>>(s, rows, cols, w_out);
+    k_scan_blocks<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum); note_launch();
+    k_scan_sums<<<1, SCAN_B, 0, st>>>(s.bsum, nb, m_dev); note_launch();
+    k_scan_add<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum); note_launch();
+    k_scatter<<<2048, 256, 0, st>>>(n, k, s); note_launch();
+    k_sort_small<<<(n + 7) / 8, 256, 0, st>>>(n, s, rows, cols, w_out); note_launch();
+    k_sort_big<<<256, 512, 0, st>>>(s, rows, cols, w_out); note_launch();
     return cudaGetLastError();
 }
 

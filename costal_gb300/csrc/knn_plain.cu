@@ -179,9 +179,9 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int s = 0; s < SLOTS; ++s) {
         const int p = s * 32 + lane;
-        if (p < cap) {
-            uint32_t j = cand_idx[(size_t)i * lstride + p];
-            if (j >= (uint32_t)n) j = 0;  // only reachable on non-finite input (reported as an error)
+        const uint32_t j = p < cap ? cand_idx[(size_t)i * lstride + p] : 0xffffffffu;
+        if (j < (uint32_t)n) {
+            // (an index ≥ n marks an empty slot: the coarse pass kept fewer than cap candidates)
             const float* xj = x + (size_t)j * d;
             double dot = 0.0;
             for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
@@ -208,7 +208,9 @@ __global__ void __launch_bounds__(256)
     // block pruning, every column of a skipped block scores at most row_ub: s_k must also beat it.
     const bool ub_bad = row_ub && s_k <= row_ub[i];
     if (ub_bad && lane == 0 && ub_fail) atomicAdd(ub_fail, 1u);
-    if ((certify && s_k <= __dadd_rn((double)tau[i], e)) || ub_bad) {
+    // fewer than k candidates kept (possible only when a coarse threshold cut the list): regather
+    const bool short_list = s_k == -CUDART_INF;
+    if ((certify && s_k <= __dadd_rn((double)tau[i], e)) || ub_bad || short_list) {
         if (lane == 0) {
             const unsigned slot = atomicAdd(fb_count, 1u);
             fb_rows[slot] = (uint32_t)i;
@@ -333,12 +335,12 @@ __global__ void __launch_bounds__(GT)
 cudaError_t launch_prep(const float* x, int n, int d, int np, int dp, double* norms, float* xsT,
                         unsigned long long* bad_row, cudaStream_t st) {
     const int blocks = (np + PREP_ROWS - 1) / PREP_ROWS;
-    k_prep<<<blocks, PREP_ROWS, 0, st>>>(x, n, d, np, dp, norms, xsT, bad_row);
+    k_prep<<<blocks, PREP_ROWS, 0, st>>>(x, n, d, np, dp, norms, xsT, bad_row); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cudaStream_t st) {
-    k_row_l2_norms_f32<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out);
+    k_row_l2_norms_f32<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out); note_launch();
     return cudaGetLastError();
 }
 
@@ -357,7 +359,7 @@ cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lst
                                          row_ub, ub_fail, eps, certify, select, rlist, rcount, out_idx, out_cos, \
                                          out_w, fb_rows, \
                                          fb_minsim,                                                           \
-                                         fb_count, max_err_bits);
+                                         fb_count, max_err_bits); note_launch();
     if (slots == 1) {
         COSTAL_RESCORE(1)
     } else if (slots == 2) {
@@ -385,13 +387,13 @@ cudaError_t launch_gather(const float* x, const float* xsT, int n, int np, int d
     cudaError_t e = cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_gather<<<grid, GT, smem, st>>>(x, xsT, n, np, d, dp, k, norms, rows, minsim, count, all_rows, select, capb,
-                                     out_idx, out_cos, out_w);
+                                     out_idx, out_cos, out_w); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_zero_pad(float* xsT, int n, int np, int dp, cudaStream_t st) {
     if (np == n) return cudaSuccess;
-    k_zero_pad_cols<<<64, 256, 0, st>>>(xsT, n, np, dp);
+    k_zero_pad_cols<<<64, 256, 0, st>>>(xsT, n, np, dp); note_launch();
     return cudaGetLastError();
 }
 

@@ -180,6 +180,8 @@ struct __align__(8) Barriers {
     uint64_t t_full[2];
     uint64_t t_empty[2];
     uint32_t tmem_base;
+    int stop_tile;         // the list position at which the CTA stops (set by the TMA warp)
+    float warp_floor[4];   // per epilogue warp: min over its rows of τ − E (never decreases)
 };
 
 // Per-query candidate buffer: BCAP = 2·LCAP entries in shared memory, [entry][query] with a row
@@ -192,24 +194,24 @@ constexpr int BSTRIDE = BLOCK_M + 1;
 // Sort one query's buffer (cntL entries) and keep its best `cap` entries at positions 0..cap-1.
 template <int SL>
 __device__ __noinline__ void flush_one(float* B_s, uint32_t* B_i, int qL, int cntL, int cap, int lane, float* tau_out) {
-    float sc[SL];
-    uint32_t id[SL];
+    uint64_t key[SL];
 #pragma unroll
     for (int s = 0; s < SL; ++s) {
         const int p = s * 32 + lane;
-        sc[s] = p < cntL ? B_s[p * BSTRIDE + qL] : -CUDART_INF_F;
-        id[s] = p < cntL ? B_i[p * BSTRIDE + qL] : 0xffffffffu;
+        key[s] = p < cntL ? order_key(B_s[p * BSTRIDE + qL], B_i[p * BSTRIDE + qL]) : PAD_KEY;
     }
-    warp_sort_f32<SL>(sc, id, lane);
+    warp_sort_keys<SL>(key, lane);
+    uint64_t kth = 0;
 #pragma unroll
     for (int s = 0; s < SL; ++s) {
         const int p = s * 32 + lane;
         if (p < cap) {
-            B_s[p * BSTRIDE + qL] = sc[s];
-            B_i[p * BSTRIDE + qL] = id[s];
+            B_s[p * BSTRIDE + qL] = key_score(key[s]);
+            B_i[p * BSTRIDE + qL] = key_index(key[s]);
         }
+        if (s == (cap - 1) >> 5) kth = key[s];
     }
-    const float t = __shfl_sync(COSTAL_FULL_MASK, sc[(cap - 1) >> 5], (cap - 1) & 31);
+    const float t = key_score(__shfl_sync(COSTAL_FULL_MASK, kth, (cap - 1) & 31));
     if (lane == 0) *tau_out = t;
     __syncwarp();
 }
@@ -226,7 +228,7 @@ __device__ __forceinline__ void flush_full(float* B_s, uint32_t* B_i, float* tau
         pend &= pend - 1;
         flush_one<SL>(B_s, B_i, qbase + L, __shfl_sync(COSTAL_FULL_MASK, cnt, L), cap, lane, &tau_s[qbase + L]);
         if (lane == L) {
-            cnt = cap;
+            cnt = min(cnt, cap);
             tau = tau_s[qbase + L];
         }
     }
@@ -314,9 +316,10 @@ template <int SLOTS>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
                 int nkb, int ksteps, int stages, int cap, const uint32_t* __restrict__ perm,
-                const uint32_t* __restrict__ lists, const uint32_t* __restrict__ counts, int ncb,
+                const uint32_t* __restrict__ lists, const float* __restrict__ list_ub,
+                const uint32_t* __restrict__ counts, int ncb, const double* __restrict__ row_eps,
                 uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
-                unsigned long long* __restrict__ timeout_flag) {
+                unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag) {
     constexpr int SL = 2 * SLOTS;  // buffer slots per lane in a flush: BCAP = 2·LCAP entries
     constexpr int BCAP = 32 * SL;
     extern __shared__ unsigned char smem_raw[];
@@ -349,6 +352,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             mbar_init(&bars->t_full[b], 1);
             mbar_init(&bars->t_empty[b], EPI_WARPS);
         }
+        bars->stop_tile = ntiles;
+        for (int w = 0; w < EPI_WARPS; ++w) bars->warp_floor[w] = -CUDART_INF_F;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == EPI_WARPS + 1) {  // the MMA warp owns the TMEM allocation
@@ -367,10 +372,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (lane == 0) {
             mbar_expect_tx(&bars->a_full, a_bytes);
             for (int kb = 0; kb < nkb; ++kb) tma_load_2d(a_tile + kb * A_KB_BYTES, &map_a, kb * KB, q0, &bars->a_full);
+            const float* my_ub = list_ub ? list_ub + (size_t)blockIdx.x * ncb : nullptr;
             for (int t = 0; t < ntiles; ++t) {
                 const int s = t % stages;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u;
                 if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) break;
+                if (t > 0 && my_ub) {
+                    // Every column of list entry t (and of all later ones: the bounds do not increase)
+                    // has cosine ≤ my_ub[t]; its coarse score is ≤ my_ub[t] + E_i. When that is below
+                    // every row's threshold τ_i, none of them can be admitted: stop here. The floors
+                    // read may be stale, i.e. lower, which only delays the stop.
+                    volatile float* wf = bars->warp_floor;
+                    const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
+                    if (my_ub[t] < fl) {
+                        *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
+                        if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
+                        mbar_arrive(&bars->b_full[s]);  // completes the phase without data (release)
+                        break;
+                    }
+                }
                 mbar_expect_tx(&bars->b_full[s], b_bytes);
                 unsigned char* dst = b_tiles + (size_t)s * b_bytes;
                 const int cb = block_of(t) * BLOCK_N;
@@ -389,6 +409,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (!mbar_wait(&bars->t_empty[buf], bph ^ 1u, timeout_flag, true)) break;
                 if (!mbar_wait(&bars->b_full[s], ph, timeout_flag, true)) break;
                 tc_fence_after();
+                if (*reinterpret_cast<volatile int*>(&bars->stop_tile) == t) {
+                    mbar_arrive(&bars->t_full[buf]);  // pass the stop on to the epilogue warps
+                    break;
+                }
                 const uint32_t b_base = smem_u32(b_tiles + (size_t)s * b_bytes);
                 const uint32_t d = tmem + (uint32_t)(buf * BLOCK_N);
                 for (int ks = 0; ks < ksteps; ++ks) {
@@ -406,6 +430,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int qbase = warp * 32;
         const int qi = qbase + lane;  // TMEM lane = query row within the block
         const int q = q0 + qi, q_lo = q0 + qbase;
+        // this row's coarse-error bound, rounded up to f32 (rows past n never hold the CTA back)
+        const float row_e = q < n ? __double2float_ru(row_eps[perm ? perm[q] : (uint32_t)q]) : 0.0f;
         float tau = -CUDART_INF_F;
         int cnt = 0;
         const uint32_t lane_addr = tmem + ((uint32_t)qbase << 16);
@@ -417,6 +443,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t bph = (uint32_t)(t >> 1) & 1u;
             if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag, false)) break;
             tc_fence_after();
+            if (*reinterpret_cast<volatile int*>(&bars->stop_tile) == t) break;
             const int c0 = block_of(t) * BLOCK_N;
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
             if (t == 0 && cap <= 32) {
@@ -467,6 +494,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bars->t_empty[buf]);
+            // the warp's floor min(τ − E) for the TMA warp's stop test (signed-int order of the f32)
+            if (list_ub) {
+                const float f = q < n ? __fsub_rd(tau, row_e) : CUDART_INF_F;
+                int key = __float_as_int(f);
+                key = __reduce_min_sync(COSTAL_FULL_MASK, key >= 0 ? key : key ^ 0x7fffffff);
+                if (lane == 0)
+                    *reinterpret_cast<volatile float*>(&bars->warp_floor[warp]) =
+                        __int_as_float(key >= 0 ? key : key ^ 0x7fffffff);
+            }
         }
         // final selection: every buffer sorted, best `cap` first
         flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, 0, cnt, tau);
@@ -474,8 +510,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (q < n) {
             const uint32_t qo = perm ? perm[q] : (uint32_t)q;
             for (int p = 0; p < cap; ++p) {
-                const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0u;
-                cand_idx[(size_t)qo * cap + p] = perm ? perm[cw] : cw;
+                // an empty slot (fewer than cap candidates) carries index 0xffffffff and score −inf
+                const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0xffffffffu;
+                cand_idx[(size_t)qo * cap + p] = cw < (uint32_t)n ? (perm ? perm[cw] : cw) : 0xffffffffu;
                 cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
             }
             tau_out[qo] = tau;
@@ -630,8 +667,8 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
     if (e != cudaSuccess) return e;
     // xsT has n_pad = ⌈n/128⌉·128 columns; rows in [n, np) are zero-filled by k_split itself.
-    k_split<<<(np + 127) / 128, 128, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax);
-    k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps);
+    k_split<<<(np + 127) / 128, 128, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax); note_launch();
+    k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps); note_launch();
     plan.n = n;
     plan.d = d;
     plan.np = np;
@@ -644,8 +681,9 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const uint32_t* counts, int ncb,
-                          uint32_t* cand_idx, float* cand_score, float* tau, unsigned long long* timeout_flag, int sm_count,
+cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const float* list_ub,
+                          const uint32_t* counts, int ncb, uint32_t* cand_idx, float* cand_score, float* tau,
+                          unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
                           cudaStream_t st) {
     (void)sm_count;
     CUtensorMap ma, mb;
@@ -662,8 +700,9 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     auto kern = cap <= 32 ? k_coarse_tc<1> : k_coarse_tc<2>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, plan.perm, lists, counts,
-                                          ncb, cand_idx, cand_score, tau, timeout_flag);
+    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, plan.perm, lists,
+                                          lists ? list_ub : nullptr, counts, ncb, plan.row_eps, cand_idx, cand_score,
+                                          tau, stopped_total, timeout_flag); note_launch();
     return cudaGetLastError();
 }
 

@@ -39,33 +39,42 @@ __host__ __device__ inline Off offsets(int F) {
 }
 
 // ---- features ---------------------------------------------------------------------------------
-// One warp per row: 8 centroid cosines per lane, a warp bitonic sort of the 256, the first 64 kept.
+// One warp per row: 8 centroid cosines per lane, a branch-free warp bitonic sort of the 256 as
+// (cosine desc, centroid asc) keys, the first 64 kept. Centroids sit in shared memory with an odd
+// row stride, so the lanes' reads of 32 different centroids hit 32 different banks.
 __global__ void k_features(const float* __restrict__ xsT, int np, int d, const float* __restrict__ cent, int K,
                            const uint32_t* __restrict__ rows, int m, float* __restrict__ feat) {
-    extern __shared__ float c_s[];  // [K][d]
-    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[e] = cent[e];
+    extern __shared__ float c_s[];  // [K][ds]
+    const int ds = d | 1;
+    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[(e / d) * ds + e % d] = cent[e];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (i >= m) return;
     const uint32_t r = rows ? rows[i] : (uint32_t)i;
     const int F = d + MLP_TOPC;
-    float sc[8];
-    uint32_t id[8];
+    float dot[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
+    for (int t = 0; t < d; ++t) {
+        const float a = xsT[(size_t)t * np + r];
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int c = s * 32 + lane;
+            if (c < K) dot[s] = fmaf(a, c_s[c * ds + t], dot[s]);
+        }
+    }
+    uint64_t key[8];
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int c = s * 32 + lane;
-        float dot = 0.0f;
-        if (c < K)
-            for (int t = 0; t < d; ++t) dot = fmaf(xsT[(size_t)t * np + r], c_s[c * d + t], dot);
-        sc[s] = c < K ? dot : -CUDART_INF_F;
-        id[s] = (uint32_t)c;
+        key[s] = c < K ? order_key(dot[s], (uint32_t)c) : PAD_KEY;
     }
-    warp_sort_f32<8>(sc, id, lane);
+    warp_sort_keys<8>(key, lane);
     float* f = feat + (size_t)i * F;
     for (int t = lane; t < d; t += 32) f[t] = xsT[(size_t)t * np + r];
-    f[d + lane] = sc[0];
-    f[d + 32 + lane] = sc[1];
+    f[d + lane] = key_score(key[0]);
+    f[d + 32 + lane] = key_score(key[1]);
 }
 
 // ---- forward (shared by inference and training) ------------------------------------------------
@@ -107,16 +116,111 @@ __device__ void forward_block(const float* __restrict__ P, int F, const float* _
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(T) k_forward(const float* __restrict__ P, int F, const float* __restrict__ feat, int m,
-                                               float* __restrict__ out) {
-    extern __shared__ float sm[];
-    float* f_s = sm;                  // [R][F]
-    float* h1_s = f_s + R * F;        // [R][T]
-    float* h2_s = h1_s + R * T;       // [R][T]
-    float* out_s = h2_s + R * T;      // [R]
-    const int r0 = blockIdx.x * R;
-    forward_block(P, F, feat, m, r0, f_s, h1_s, h2_s, out_s);
-    if (threadIdx.x < R && r0 + threadIdx.x < m) out[r0 + threadIdx.x] = out_s[threadIdx.x];
+// ---- inference ----------------------------------------------------------------------------------
+// Persistent CTAs of 256 threads: the weights, transposed, stay in shared memory while the CTA walks
+// 64-row tiles. Thread (ty, tx) = (tid / 16, tid % 16) holds a 4-row × 8-unit register tile: per
+// input feature one float4 of the (transposed) activations and two float4 of weights feed 32 FMAs.
+// Every hidden unit's sum runs bias first, then the inputs in order, like forward_block; the output
+// adds 16 partial sums of 8 units in a fixed tree.
+constexpr int IR = 64;        // rows per tile
+constexpr int IT = 256;       // threads
+constexpr int IRS = IR + 4;   // row stride of the transposed activations (float4-aligned)
+
+__global__ void __launch_bounds__(IT, 1) k_infer(const float* __restrict__ P, int F, const float* __restrict__ feat,
+                                                 int m, float* __restrict__ out) {
+    extern __shared__ __align__(16) float sm[];
+    float* w1t = sm;                            // [F][H]
+    float* w2t = w1t + (size_t)F * MLP_H;       // [H][H]
+    float* b1 = w2t + MLP_H * MLP_H;            // [H]
+    float* b2 = b1 + MLP_H;                     // [H]
+    float* w3 = b2 + MLP_H;                     // [H]
+    float* ft = w3 + MLP_H;                     // [F][IRS] features, transposed
+    float* h1t = ft + (size_t)F * IRS;          // [H][IRS] layer-1 activations, transposed
+    const Off o = offsets(F);
+    const int tid = threadIdx.x;
+    for (int e = tid; e < MLP_H * F; e += IT) {
+        const int u = e / F, t = e % F;
+        w1t[t * MLP_H + u] = P[o.w1 + e];
+    }
+    for (int e = tid; e < MLP_H * MLP_H; e += IT) {
+        const int u = e / MLP_H, t = e % MLP_H;
+        w2t[t * MLP_H + u] = P[o.w2 + e];
+    }
+    if (tid < MLP_H) {
+        b1[tid] = P[o.b1 + tid];
+        b2[tid] = P[o.b2 + tid];
+        w3[tid] = P[o.w3 + tid];
+    }
+    const float b3 = P[o.b3];
+    const int ty = tid >> 4, tx = tid & 15;
+    const int ntiles = (m + IR - 1) / IR;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int r0 = tile * IR;
+        __syncthreads();  // the previous tile's readers of ft / h1t are done (and the weights loaded)
+        for (int e = tid; e < IR * F; e += IT) {
+            const int r = e % IR, t = e / IR;
+            ft[t * IRS + r] = r0 + r < m ? feat[(size_t)(r0 + r) * F + t] : 0.0f;
+        }
+        __syncthreads();
+        float acc[4][8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float b = b1[tx * 8 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i][j] = b;
+        }
+        for (int t = 0; t < F; ++t) {
+            const float4 a = *reinterpret_cast<const float4*>(ft + t * IRS + ty * 4);
+            const float4 wa = *reinterpret_cast<const float4*>(w1t + t * MLP_H + tx * 8);
+            const float4 wb = *reinterpret_cast<const float4*>(w1t + t * MLP_H + tx * 8 + 4);
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            *reinterpret_cast<float4*>(h1t + (tx * 8 + j) * IRS + ty * 4) =
+                make_float4(fmaxf(acc[0][j], 0.0f), fmaxf(acc[1][j], 0.0f), fmaxf(acc[2][j], 0.0f),
+                            fmaxf(acc[3][j], 0.0f));
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float b = b2[tx * 8 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i][j] = b;
+        }
+        for (int t = 0; t < MLP_H; ++t) {
+            const float4 a = *reinterpret_cast<const float4*>(h1t + t * IRS + ty * 4);
+            const float4 wa = *reinterpret_cast<const float4*>(w2t + t * MLP_H + tx * 8);
+            const float4 wb = *reinterpret_cast<const float4*>(w2t + t * MLP_H + tx * 8 + 4);
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
+        }
+        // output layer: each thread's 8 units, then the 16 threads of a row group in a fixed tree
+        float p[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float z = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) z = fmaf(w3[tx * 8 + j], fmaxf(acc[i][j], 0.0f), z);
+            p[i] = z;
+        }
+#pragma unroll
+        for (int off = 1; off < 16; off <<= 1)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) p[i] += __shfl_xor_sync(COSTAL_FULL_MASK, p[i], off);
+        if (tx == 0)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (r0 + ty * 4 + i < m) out[r0 + ty * 4 + i] = b3 + p[i];
+    }
 }
 
 // ---- backward ----------------------------------------------------------------------------------
@@ -230,25 +334,32 @@ __global__ void k_block_min(const float* __restrict__ pred, const uint32_t* __re
 
 // ---- launchers ----------------------------------------------------------------------------------
 
-static size_t fwd_smem(int F) { return (size_t)(R * F + 2 * R * T + R) * 4; }
 static size_t grad_smem(int F) { return (size_t)(R * F + 4 * R * T + 2 * R) * 4; }
 
 cudaError_t features(const float* xsT, int np, int d, const float* centroids, int K, const uint32_t* rows, int m,
                      float* feat, cudaStream_t st) {
     if (m == 0) return cudaSuccess;
-    const size_t smem = (size_t)K * d * 4;
+    const size_t smem = (size_t)K * (d | 1) * 4;
     cudaError_t e = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_features<<<(m + 7) / 8, 256, smem, st>>>(xsT, np, d, centroids, K, rows, m, feat);
+    k_features<<<(m + 7) / 8, 256, smem, st>>>(xsT, np, d, centroids, K, rows, m, feat); note_launch();
     return cudaGetLastError();
+}
+
+static size_t infer_smem(int F) {
+    return ((size_t)F * MLP_H + MLP_H * MLP_H + 3 * MLP_H + (size_t)F * IRS + (size_t)MLP_H * IRS) * 4;
 }
 
 cudaError_t forward(const float* params, int F, const float* feat, int m, float* out, cudaStream_t st) {
     if (m == 0) return cudaSuccess;
-    const size_t smem = fwd_smem(F);
-    cudaError_t e = cudaFuncSetAttribute(k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = infer_smem(F);
+    cudaError_t e = cudaFuncSetAttribute(k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_forward<<<(m + R - 1) / R, T, smem, st>>>(params, F, feat, m, out);
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int tiles = (m + IR - 1) / IR;
+    k_infer<<<tiles < sms ? tiles : sms, IT, smem, st>>>(params, F, feat, m, out); note_launch();
     return cudaGetLastError();
 }
 
@@ -258,24 +369,24 @@ cudaError_t gradient(const float* params, int F, const float* feat, const float*
     const size_t smem = grad_smem(F);
     cudaError_t e = cudaFuncSetAttribute(k_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_grad_partial<<<groups, T, smem, st>>>(params, F, feat, y, m, quantile, partial);
-    k_grad_reduce<<<128, 256, 0, st>>>(partial, groups, mlp_param_count(F), grad);
+    k_grad_partial<<<groups, T, smem, st>>>(params, F, feat, y, m, quantile, partial); note_launch();
+    k_grad_reduce<<<128, 256, 0, st>>>(partial, groups, mlp_param_count(F), grad); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t adam(float* params, const float* grad, float* m1, float* m2, size_t np, float lr, int t, cudaStream_t st) {
     const float bc1 = 1.0f - powf(0.9f, (float)t), bc2 = 1.0f - powf(0.999f, (float)t);
-    k_adam<<<128, 256, 0, st>>>(params, grad, m1, m2, np, lr, bc1, bc2);
+    k_adam<<<128, 256, 0, st>>>(params, grad, m1, m2, np, lr, bc1, bc2); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t round_bf16(const float* params, float* params_bf, size_t np, cudaStream_t st) {
-    k_round_bf16<<<64, 256, 0, st>>>(params, params_bf, np);
+    k_round_bf16<<<64, 256, 0, st>>>(params, params_bf, np); note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t block_min(const float* pred_orig, const uint32_t* perm, int n, float* tq, cudaStream_t st) {
-    k_block_min<<<(n + prune::QB - 1) / prune::QB, prune::QB, 0, st>>>(pred_orig, perm, n, tq);
+    k_block_min<<<(n + prune::QB - 1) / prune::QB, prune::QB, 0, st>>>(pred_orig, perm, n, tq); note_launch();
     return cudaGetLastError();
 }
 

@@ -22,6 +22,11 @@
 
 #include "costal_gb300.h"
 
+namespace costal {
+void note_launch();
+}
+using costal::note_launch;
+
 namespace {
 
 constexpr size_t NOALLOC_HEADER_BYTES = 256;  // first-bad-index flag, cleared at every call
@@ -126,8 +131,8 @@ extern "C" int costal_reweight_jaccard_device_noalloc(const int32_t* d_idx, uint
         put_err(err, errlen, std::string("cudaMemsetAsync failed: ") + cudaGetErrorString(e));
         return COSTAL_ECUDA;
     }
-    k_sort_rows_checked<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(d_idx, (int)n, (int)k, sorted, first_bad);
-    k_jaccard_checked<<<1024, 256, 0, st>>>(d_idx, sorted, (int)n, (int)k, d_out);
+    k_sort_rows_checked<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(d_idx, (int)n, (int)k, sorted, first_bad); note_launch();
+    k_jaccard_checked<<<1024, 256, 0, st>>>(d_idx, sorted, (int)n, (int)k, d_out); note_launch();
     unsigned long long bad = 0;
     int32_t bad_val = 0;
     if ((e = cudaGetLastError()) != cudaSuccess ||

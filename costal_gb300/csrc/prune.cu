@@ -232,13 +232,14 @@ __device__ __forceinline__ double block_ub(const double* cq, double rq, const do
 }
 
 // One CTA per query block: the upper bound against every column block, the blocks kept (UB ≥ t_Q)
-// sorted by UB descending (shared-memory bitonic sort when they fit, else in block order), and the
-// largest UB of a skipped block.
+// sorted by UB descending with their bounds (shared-memory bitonic sort when they fit, else in block
+// order with bounds +inf), and the largest UB of a skipped block.
 __global__ void __launch_bounds__(LIST_T)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
                   const double* __restrict__ ccenter, const double* __restrict__ cradius, int nqb, int ncb, int d,
-                  const float* __restrict__ tq, uint32_t* __restrict__ lists, uint32_t* __restrict__ counts,
-                  float* __restrict__ ub_skip, unsigned long long* __restrict__ skipped_total) {
+                  const float* __restrict__ tq, uint32_t* __restrict__ lists, float* __restrict__ list_ub,
+                  uint32_t* __restrict__ counts, float* __restrict__ ub_skip,
+                  unsigned long long* __restrict__ skipped_total) {
     extern __shared__ unsigned char sm[];
     float* key = reinterpret_cast<float*>(sm);              // [8192]
     uint32_t* id = reinterpret_cast<uint32_t*>(key + 8192);  // [8192]
@@ -256,6 +257,7 @@ __global__ void __launch_bounds__(LIST_T)
     const float t = tq ? tq[Q] : -CUDART_INF_F;
     const bool sortable = ncb <= 8192;
     uint32_t* out = lists + (size_t)Q * ncb;
+    float* out_ub = list_ub + (size_t)Q * ncb;
     for (int b = threadIdx.x; b < ncb; b += blockDim.x) {
         const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
         float ubf = (float)ub;
@@ -297,14 +299,20 @@ __global__ void __launch_bounds__(LIST_T)
                 __syncthreads();
             }
         }
-        for (unsigned b = threadIdx.x; b < kept; b += blockDim.x) out[b] = id[b];
+        for (unsigned b = threadIdx.x; b < kept; b += blockDim.x) {
+            out[b] = id[b];
+            out_ub[b] = key[b];
+        }
     } else if (threadIdx.x == 0) {
         unsigned c = 0;
         for (int b = 0; b < ncb; ++b) {
             const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
             float ubf = (float)ub;
             if ((double)ubf < ub) ubf = nextafterf(ubf, CUDART_INF_F);
-            if (ubf >= t) out[c++] = (uint32_t)b;
+            if (ubf >= t) {
+                out_ub[c] = CUDART_INF_F;  // block order: the bounds do not decrease along the list
+                out[c++] = (uint32_t)b;
+            }
         }
     }
     __syncthreads();
@@ -340,7 +348,7 @@ size_t workspace_bytes(int n, int d) {
     const size_t nqb = (size_t)(n + QB - 1) / QB, ncb = (size_t)(n + CB - 1) / CB;
     const size_t m = (size_t)(n < SAMPLE ? n : SAMPLE), nch = (size_t)(n + CHUNK - 1) / CHUNK;
     return a256(n * 4ull) * 2 + a256((size_t)K_CENTROIDS * d * 4) + a256(nqb * d * 8) + a256(nqb * 8) +
-           a256(ncb * d * 8) + a256(ncb * 8) + a256(nqb * ncb * 4) + a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) +
+           a256(ncb * d * 8) + a256(ncb * 8) + 2 * a256(nqb * ncb * 4) + a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) +
            a256(nqb * 4) + a256(m * d * 4) + a256(m * 4) + a256(nch * K_CENTROIDS * 4) + a256((K_CENTROIDS + 1) * 4) +
            a256(m * 4) + 4096;
 }
@@ -392,6 +400,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     P.ccenter = reinterpret_cast<double*>(take((size_t)ncb * d * 8));
     P.cradius = reinterpret_cast<double*>(take((size_t)ncb * 8));
     P.lists = reinterpret_cast<uint32_t*>(take((size_t)nqb * ncb * 4));
+    P.list_ub = reinterpret_cast<float*>(take((size_t)nqb * ncb * 4));
     P.counts = reinterpret_cast<uint32_t*>(take((size_t)nqb * 4));
     P.ub_skip = reinterpret_cast<float*>(take((size_t)nqb * 4));
     P.row_ub = reinterpret_cast<double*>(take(n * 8ull));
@@ -407,20 +416,20 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     const size_t csm = (size_t)K * d * 4;
     cudaError_t e = cudaFuncSetAttribute(k_assign, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
     if (e != cudaSuccess) return e;
-    k_sample_idx<<<(m + 255) / 256, 256, 0, st>>>(S.sample_idx, m, n);
-    k_gather_rows<<<1024, 256, 0, st>>>(xsT, np, d, S.sample_idx, m, S.sample_rows);
-    k_init_centroids<<<(K * d + 255) / 256, 256, 0, st>>>(S.sample_rows, m, d, K, P.centroids);
+    k_sample_idx<<<(m + 255) / 256, 256, 0, st>>>(S.sample_idx, m, n); note_launch();
+    k_gather_rows<<<1024, 256, 0, st>>>(xsT, np, d, S.sample_idx, m, S.sample_rows); note_launch();
+    k_init_centroids<<<(K * d + 255) / 256, 256, 0, st>>>(S.sample_rows, m, d, K, P.centroids); note_launch();
     for (int it = 0; it < LLOYD_STEPS; ++it) {
         k_assign<<<(m + KM_BLOCK - 1) / KM_BLOCK, KM_BLOCK, csm, st>>>(S.sample_rows, nullptr, np, m, d, P.centroids, K,
-                                                                         S.sample_assign);
-        k_centroid_update<<<K, UPD_T, 0, st>>>(S.sample_rows, m, d, S.sample_assign, P.centroids);
+                                                                         S.sample_assign); note_launch();
+        k_centroid_update<<<K, UPD_T, 0, st>>>(S.sample_rows, m, d, S.sample_assign, P.centroids); note_launch();
     }
-    k_assign<<<(n + KM_BLOCK - 1) / KM_BLOCK, KM_BLOCK, csm, st>>>(nullptr, xsT, np, n, d, P.centroids, K, P.cell);
-    k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist);
-    k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start);
-    k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm);
-    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius);
-    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius);
+    k_assign<<<(n + KM_BLOCK - 1) / KM_BLOCK, KM_BLOCK, csm, st>>>(nullptr, xsT, np, n, d, P.centroids, K, P.cell); note_launch();
+    k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist); note_launch();
+    k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start); note_launch();
+    k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm); note_launch();
+    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius); note_launch();
+    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius); note_launch();
     return cudaGetLastError();
 }
 
@@ -429,8 +438,8 @@ cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t
     cudaError_t e = cudaFuncSetAttribute(k_block_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_block_lists<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter, P.cradius, P.nqb, P.ncb, P.d, P.tq,
-                                              P.lists, P.counts, P.ub_skip, skipped_total);
-    k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub);
+                                              P.lists, P.list_ub, P.counts, P.ub_skip, skipped_total); note_launch();
+    k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub); note_launch();
     return cudaGetLastError();
 }
 

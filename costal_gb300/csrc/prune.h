@@ -24,6 +24,7 @@ struct Plan {
     double* ccenter;     // [ncb][d]
     double* cradius;     // [ncb]
     uint32_t* lists;     // [nqb][ncb] kept column blocks, nearest first
+    float* list_ub;      // [nqb][ncb] the bound of each list entry (non-increasing; +inf when unsorted)
     uint32_t* counts;    // [nqb]
     float* ub_skip;      // [nqb]
     double* row_ub;      // [n] (original order) pruning floor of the certificate

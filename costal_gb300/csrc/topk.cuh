@@ -55,6 +55,56 @@ __device__ __forceinline__ void list_insert(float (&ls)[SLOTS], uint32_t (&li)[S
 }
 
 
+// (score, index) as one 64-bit key whose unsigned order is `better`: the f32 score mapped to an
+// order-preserving u32 in the high word, the complemented index in the low word (smaller index →
+// larger key). Padding (−inf, 0xffffffff) maps to the smallest keys.
+__device__ __forceinline__ uint64_t order_key(float s, uint32_t i) {
+    const uint32_t u = __float_as_uint(s);
+    const uint32_t h = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((uint64_t)h << 32) | (uint64_t)(~i);
+}
+__device__ __forceinline__ float key_score(uint64_t k) {
+    const uint32_t h = (uint32_t)(k >> 32);
+    return __uint_as_float((h & 0x80000000u) ? (h & 0x7fffffffu) : ~h);
+}
+__device__ __forceinline__ uint32_t key_index(uint64_t k) { return ~(uint32_t)k; }
+constexpr uint64_t PAD_KEY = 0x007fffff00000000ull;  // order_key(−inf, 0xffffffff)
+
+// Bitonic sort of warp-distributed 64-bit keys (position p = s·32 + lane) into descending order.
+// Every compare-exchange is a max/min pair and a select: no branch, so the warp never diverges
+// between its shuffles.
+template <int SL>
+__device__ __forceinline__ void warp_sort_keys(uint64_t (&v)[SL], int lane) {
+    constexpr int N = 32 * SL;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+#pragma unroll
+                for (int s = 0; s < SL; ++s) {
+                    const int t = s ^ (stride >> 5);
+                    if (t > s) {
+                        const bool desc = ((s * 32 + lane) & size) == 0;
+                        const uint64_t a = v[s], b = v[t];
+                        const uint64_t hi = a > b ? a : b, lo = a > b ? b : a;
+                        v[s] = desc ? hi : lo;
+                        v[t] = desc ? lo : hi;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < SL; ++s) {
+                    const uint64_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[s], stride);
+                    const bool keep_max = ((lane & stride) == 0) == (((s * 32 + lane) & size) == 0);
+                    const uint64_t hi = v[s] > o ? v[s] : o, lo = v[s] > o ? o : v[s];
+                    v[s] = keep_max ? hi : lo;
+                }
+            }
+        }
+    }
+}
+
 // Bitonic sort of a warp-distributed array (position p = s·32 + lane) into (score desc, index asc).
 template <int SL>
 __device__ __forceinline__ void warp_sort_f32(float (&sc)[SL], uint32_t (&id)[SL], int lane) {

@@ -50,7 +50,8 @@ typedef struct costal_knn_opts {
     uint32_t row_block;    /* accepted for compatibility (knn.rs:35-37); speed-only, 0 = derive */
     uint32_t col_block;    /* idem */
     int32_t sort_by_norm;  /* idem (knn.rs:41): output-independent */
-    int32_t prune;         /* idem (knn.rs:44): output-independent */
+    int32_t prune;         /* idem (knn.rs:44): output-independent; on the bf16 backend it enables the
+                              exact early stop of each query block's column list */
     int32_t learned_prune; /* 1 = use the trained block-pruning model if one is loaded (bf16 backend) */
 } costal_knn_opts;
 
@@ -67,10 +68,16 @@ typedef struct costal_knn_stats {
     double max_coarse_err;     /* max |coarse score - f64 rescored score| over all kept candidates */
     double ms_prep, ms_coarse, ms_rescore, ms_fallback, ms_total; /* CUDA-event times of the stages */
     double ms_order;           /* bf16 backend: locality order, block bounds and lists (inside ms_total) */
+    double ms_kernel;          /* the coarse tile + selection kernel alone (inside ms_coarse) */
+    uint64_t blocks_stopped;   /* bf16 backend: list blocks left out because every row's threshold
+                                  already exceeded their bound (exact; no certificate needed) */
 } costal_knn_stats;
 
 /* ---- module surface (crates/costal-py/src/lib.rs:80-102, 430-446) ---------------------------- */
 const char* costal_version(void);   /* replaces env!("CARGO_PKG_VERSION") of lib.rs:450 */
+/* GB300 addition, no reference counterpart: the number of CUDA kernels this library has launched
+   in this process (a monotone counter; take differences around a call). */
+unsigned long long costal_launch_count(void);
 int costal_device_ok(char* err, size_t errlen);  /* 0 when a usable sm_103 device is present */
 /* lib.rs:94-102 (costal_core::row_l2_norms, crates/costal-core/src/lib.rs:34-47): f32 row norms. */
 int costal_row_l2_norms(const float* x, uint64_t n, uint32_t d, float* out, char* err, size_t errlen);
