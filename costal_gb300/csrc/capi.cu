@@ -65,6 +65,7 @@ struct Context {
     DevBuf x, norms, xsT, cand_idx, cand_score, tau, out_idx, out_cos, out_w, fb_rows, fb_minsim, misc;
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
+    DevBuf part_idx, part_score, part_tau;
     MlpState mlp;
 };
 
@@ -245,18 +246,31 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                               &dm->prune_fail_count, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx, d_cos, d_w,
                               c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
                               &dm->max_err_bits, s));
-            if (dp > 64 || coarse_fp32_smem(dp, cap) > 227 * 1024)
-                throw Fail{COSTAL_EUNSUPPORTED, "d too large for the FP32 re-run of uncertified rows"};
-            CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, c.tc_rows.as<uint32_t>(), &dm->tc_fail_count,
-                                  c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
-            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0,
-                              c.tc_rows.as<uint32_t>(), &dm->tc_fail_count, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(),
-                              c.fb_minsim.as<double>(), &dm->fb_count, nullptr, s));
+            if (coarse_fp32_smem(dp, cap) > 227 * 1024)
+                throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 re-run of uncertified rows"};
+            // How many rows failed decides the re-run's shape (few rows: the columns split across CTAs).
+            CK(cudaMemcpyAsync(&c.h_misc->tc_fail_count, &dm->tc_fail_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                               s));
+            CK(cudaStreamSynchronize(s));
+            const int nfail = (int)c.h_misc->tc_fail_count;
+            if (nfail > 0) {
+                const int segs = coarse_fp32_segments(nfail, np, cap, c.sm_count);
+                if (segs > 1) {
+                    CK(ensure(c.part_idx, (size_t)segs * nfail * cap * 4));
+                    CK(ensure(c.part_score, (size_t)segs * nfail * cap * 4));
+                    CK(ensure(c.part_tau, (size_t)segs * nfail * 4));
+                }
+                CK(launch_coarse_fp32_split(c.xsT.as<float>(), n, np, dp, cap, cap, c.tc_rows.as<uint32_t>(),
+                                            &dm->tc_fail_count, nfail, segs, c.part_idx.as<uint32_t>(),
+                                            c.part_score.as<float>(), c.part_tau.as<float>(), c.cand_idx.as<uint32_t>(),
+                                            c.cand_score.as<float>(), c.tau.as<float>(), s));
+                CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                  c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0,
+                                  c.tc_rows.as<uint32_t>(), &dm->tc_fail_count, d_idx, d_cos, d_w,
+                                  c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->fb_count, nullptr, s));
+            }
             CK(cudaEventRecord(c.ev[3], s));
         } else {
-            if (dp > 64)
-                throw Fail{COSTAL_EUNSUPPORTED, "d > 64 is not supported by the FP32 coarse kernel yet"};
             if (coarse_fp32_smem(dp, cap) > 227 * 1024)
                 throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 coarse kernel"};
             CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, nullptr, nullptr, c.cand_idx.as<uint32_t>(),
@@ -281,6 +295,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaStreamSynchronize(s));
     const Misc& hm = *c.h_misc;
     if (hm.bad_row != ~0ull) throw Fail{COSTAL_EINVAL, "row " + std::to_string(hm.bad_row) + " contains NaN or inf"};
+    if (hm.timeout_flag == 2) throw Fail{COSTAL_ECUDA, "internal error: a column-block list entry out of range"};
     if (hm.timeout_flag) throw Fail{COSTAL_ETIMEOUT, "a bounded device wait in the tensor-core kernel gave up"};
     if (st) {
         st->fallback_rows = hm.fb_count;

@@ -16,6 +16,8 @@
 // tile row recomputed by its warp in the same FMA order and inserted column by column.
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math_constants.h>
 #include <stdint.h>
 
@@ -50,10 +52,120 @@ __device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsign
     return d;
 }
 
+// The CTA's lists out: by row (lstride per row), or, with column segments (part_stride > 0), by
+// list slot into segment blockIdx.y's part of the output (cap per slot), for k_merge_parts.
+template <class RowOf>
+__device__ __forceinline__ void write_lists(const float* L_s, const uint32_t* L_i, const float* tau_s, int lcap, int cap,
+                                            int lstride, int n, int nq, int q0, int part_stride, RowOf row_of,
+                                            uint32_t* cand_idx, float* cand_score, float* tau_out) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < BM * cap; e += NT) {
+        const int qi = e / cap, p = e % cap, q = row_of(qi);
+        if (q < 0 || q >= n) continue;
+        const size_t o = part_stride ? ((size_t)blockIdx.y * part_stride + q0 + qi) * cap + p : (size_t)q * lstride + p;
+        cand_idx[o] = L_i[qi * lcap + p];
+        cand_score[o] = L_s[qi * lcap + p];
+    }
+    for (int qi = tid; qi < BM; qi += NT) {
+        const int q = row_of(qi);
+        if (q < 0 || q >= n) continue;
+        tau_out[part_stride ? (size_t)blockIdx.y * part_stride + q0 + qi : (size_t)q] = tau_s[qi];
+    }
+    (void)nq;
+}
+
+// The selection of one 128 × 128 tile, shared by both FP32 kernels: the admission test of the
+// thread's 8 × 8 scores against each query's τ at the tile start, the per-query buffer, and the
+// warp-local merges into the top-cap lists. `recompute(qi, cl)` returns the score of query slot qi
+// and tile column cl with the same FMA order as the main loop (used when a buffer overflows).
+template <int SLOTS, class RowOf, class Recompute>
+__device__ __forceinline__ void select_tile(const float (&acc)[8][8], int c0, int n, int cap, float* L_s, uint32_t* L_i,
+                                            float* buf_s, uint32_t* buf_i, int* cnt_s, int* len_s, float* tau_s,
+                                            int warp, int lane, int tx, int ty, RowOf row_of, Recompute recompute) {
+    constexpr int LCAP = 32 * SLOTS;
+    auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
+    auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
+    // Admission test against each query's τ at the tile start: a max-tree per register row.
+    bool hit = false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float m01 = fmaxf(acc[i][0], acc[i][1]), m23 = fmaxf(acc[i][2], acc[i][3]);
+        const float m45 = fmaxf(acc[i][4], acc[i][5]), m67 = fmaxf(acc[i][6], acc[i][7]);
+        hit |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > tau_s[qi_of(i)];
+    }
+    if (hit) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const float th = tau_s[qi_of(i)];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (acc[i][j] > th) {
+                    const int qi = qi_of(i), col = c0 + cj_of(j);
+                    if (col < n && col != row_of(qi)) {
+                        const int pos = atomicAdd(&cnt_s[qi], 1);
+                        if (pos < BUF) {
+                            buf_s[qi * BUF + pos] = acc[i][j];
+                            buf_i[qi * BUF + pos] = (uint32_t)col;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (__any_sync(COSTAL_FULL_MASK, hit)) {
+        // Warp-local merge of this warp's 16 queries (8w..8w+7 and 64+8w..64+8w+7).
+        for (int qq = 0; qq < 16; ++qq) {
+            const int qi = qq < 8 ? 8 * warp + qq : 64 + 8 * warp + (qq - 8);
+            const int c = cnt_s[qi];
+            if (c == 0) continue;
+            const int q = row_of(qi);
+            float ls[SLOTS];
+            uint32_t li[SLOTS];
+#pragma unroll
+            for (int s = 0; s < SLOTS; ++s) {
+                ls[s] = L_s[qi * LCAP + s * 32 + lane];
+                li[s] = L_i[qi * LCAP + s * 32 + lane];
+            }
+            int len = len_s[qi];
+            if (c <= BUF) {
+                for (int e = 0; e < c; ++e)
+                    list_insert<SLOTS>(ls, li, len, cap, buf_s[qi * BUF + e], buf_i[qi * BUF + e], lane);
+            } else {
+                const float th0 = tau_s[qi];
+                for (int cc = 0; cc < BN / 32; ++cc) {
+                    const int cl = cc * 32 + lane, col = c0 + cl;
+                    const float sv = recompute(qi, cl);
+                    unsigned m = __ballot_sync(COSTAL_FULL_MASK, col < n && col != q && sv > th0);
+                    while (m) {
+                        const int src = __ffs(m) - 1;
+                        m &= m - 1;
+                        const float v = __shfl_sync(COSTAL_FULL_MASK, sv, src);
+                        list_insert<SLOTS>(ls, li, len, cap, v, (uint32_t)(c0 + cc * 32 + src), lane);
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < SLOTS; ++s) {
+                L_s[qi * LCAP + s * 32 + lane] = ls[s];
+                L_i[qi * LCAP + s * 32 + lane] = li[s];
+            }
+            const float worst = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
+            __syncwarp();
+            if (lane == 0) {
+                len_s[qi] = len;
+                tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
+                cnt_s[qi] = 0;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 template <int SLOTS, int DPC>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp_rt, int cap, int lstride,
-                  const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount,
+                  const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
                   uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
     constexpr int LCAP = 32 * SLOTS;
     const int dp = DPC ? DPC : dp_rt;
@@ -75,7 +187,9 @@ __global__ void __launch_bounds__(NT, 1)
     const int nq = qlist ? min(BM, (int)*qcount - q0) : BM;
     if (nq <= 0) return;
     auto row_of = [&](int qi) -> int { return qlist ? (qi < nq ? (int)qlist[q0 + qi] : -1) : q0 + qi; };
-    const int ntiles = np / BN;
+    // Column segment blockIdx.y of gridDim.y (one segment: all tiles).
+    const int all_tiles = np / BN, tps = (all_tiles + gridDim.y - 1) / gridDim.y;
+    const int tile0 = blockIdx.y * tps, ntiles = max(0, min(all_tiles, tile0 + tps) - tile0);
 
     auto load_tile = [&](float* dst, int c0) {
         for (int ch = tid; ch < dp * (BN / 4); ch += NT) {
@@ -91,9 +205,9 @@ __global__ void __launch_bounds__(NT, 1)
     } else {
         load_tile(A_s, q0);
     }
-    load_tile(B_s, 0);
+    if (ntiles > 0) load_tile(B_s, tile0 * BN);
     cp_async_commit();
-    if (ntiles > 1) load_tile(B_s + (size_t)dp * BN, BN);
+    if (ntiles > 1) load_tile(B_s + (size_t)dp * BN, (tile0 + 1) * BN);
     cp_async_commit();
     for (int q = tid; q < BM; q += NT) {
         cnt_s[q] = 0;
@@ -107,16 +221,13 @@ __global__ void __launch_bounds__(NT, 1)
         L_i[e] = 0u;
     }
 
-    auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
-    auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
-
-    for (int tile = 0; tile < ntiles; ++tile) {
+    for (int tl = 0; tl < ntiles; ++tl) {
         cp_async_wait<1>();
-        __syncthreads();  // tile's stage landed for every thread; stage (tile+2)%3 is free again
-        if (tile + 2 < ntiles) load_tile(B_s + (size_t)((tile + 2) % STAGES) * dp * BN, (tile + 2) * BN);
+        __syncthreads();  // tile's stage landed for every thread; stage (tl+2)%3 is free again
+        if (tl + 2 < ntiles) load_tile(B_s + (size_t)((tl + 2) % STAGES) * dp * BN, (tile0 + tl + 2) * BN);
         cp_async_commit();
-        const float* Bst = B_s + (size_t)(tile % STAGES) * dp * BN;
-        const int c0 = tile * BN;
+        const float* Bst = B_s + (size_t)(tl % STAGES) * dp * BN;
+        const int c0 = (tile0 + tl) * BN;
 
         float acc[8][8];
 #if COSTAL_FP32_PAIRED
@@ -166,97 +277,160 @@ __global__ void __launch_bounds__(NT, 1)
         }
 #endif
 
-        // Admission test against each query's τ at the tile start: a max-tree per register row.
-        bool hit = false;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const float m01 = fmaxf(acc[i][0], acc[i][1]), m23 = fmaxf(acc[i][2], acc[i][3]);
-            const float m45 = fmaxf(acc[i][4], acc[i][5]), m67 = fmaxf(acc[i][6], acc[i][7]);
-            hit |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > tau_s[qi_of(i)];
-        }
-        if (hit) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const float th = tau_s[qi_of(i)];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (acc[i][j] > th) {
-                        const int qi = qi_of(i), col = c0 + cj_of(j);
-                        if (col < n && col != row_of(qi)) {
-                            const int pos = atomicAdd(&cnt_s[qi], 1);
-                            if (pos < BUF) {
-                                buf_s[qi * BUF + pos] = acc[i][j];
-                                buf_i[qi * BUF + pos] = (uint32_t)col;
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        __syncwarp();
-        if (__any_sync(COSTAL_FULL_MASK, hit)) {
-            // Warp-local merge of this warp's 16 queries (8w..8w+7 and 64+8w..64+8w+7).
-            for (int qq = 0; qq < 16; ++qq) {
-                const int qi = qq < 8 ? 8 * warp + qq : 64 + 8 * warp + (qq - 8);
-                const int c = cnt_s[qi];
-                if (c == 0) continue;
-                const int q = row_of(qi);
-                float ls[SLOTS];
-                uint32_t li[SLOTS];
-#pragma unroll
-                for (int s = 0; s < SLOTS; ++s) {
-                    ls[s] = L_s[qi * LCAP + s * 32 + lane];
-                    li[s] = L_i[qi * LCAP + s * 32 + lane];
-                }
-                int len = len_s[qi];
-                if (c <= BUF) {
-                    for (int e = 0; e < c; ++e)
-                        list_insert<SLOTS>(ls, li, len, cap, buf_s[qi * BUF + e], buf_i[qi * BUF + e], lane);
-                } else {
-                    const float th0 = tau_s[qi];
-                    for (int cc = 0; cc < BN / 32; ++cc) {
-                        const int cl = cc * 32 + lane, col = c0 + cl;
-                        float sv = 0.0f;
+        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, warp, lane, tx, ty, row_of,
+                           [&](int qi, int cl) {
+                               float sv = 0.0f;
 #pragma unroll(DPC ? DPC : 4)
-                        for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
-                        unsigned m = __ballot_sync(COSTAL_FULL_MASK, col < n && col != q && sv > th0);
-                        while (m) {
-                            const int src = __ffs(m) - 1;
-                            m &= m - 1;
-                            const float v = __shfl_sync(COSTAL_FULL_MASK, sv, src);
-                            list_insert<SLOTS>(ls, li, len, cap, v, (uint32_t)(c0 + cc * 32 + src), lane);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int s = 0; s < SLOTS; ++s) {
-                    L_s[qi * LCAP + s * 32 + lane] = ls[s];
-                    L_i[qi * LCAP + s * 32 + lane] = li[s];
-                }
-                const float worst = __shfl_sync(COSTAL_FULL_MASK, ls[(cap - 1) >> 5], (cap - 1) & 31);
-                __syncwarp();
-                if (lane == 0) {
-                    len_s[qi] = len;
-                    tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
-                    cnt_s[qi] = 0;
-                }
-            }
-            __syncwarp();
-        }
+                               for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
+                               return sv;
+                           });
     }
     cp_async_wait<0>();
     __syncthreads();
-    for (int e = tid; e < BM * cap; e += NT) {
-        const int qi = e / cap, p = e % cap, q = row_of(qi);
-        if (q >= 0 && q < n) {
-            cand_idx[(size_t)q * lstride + p] = L_i[qi * LCAP + p];
-            cand_score[(size_t)q * lstride + p] = L_s[qi * LCAP + p];
+    write_lists(L_s, L_i, tau_s, LCAP, cap, lstride, n, nq, q0, part_stride, row_of, cand_idx, cand_score, tau_out);
+}
+
+// The same pass for any depth: the dimensions stream through the 3-stage ring in chunks of KC rows
+// of the transposed copy (query chunk and column chunk per stage), and the 8 × 8 register tile
+// accumulates across the chunks of a tile in dimension order, so every score is the same FMA chain
+// as in k_coarse_fp32. A query whose buffer overflows is recomputed from global memory.
+template <int SLOTS, int KC>
+__global__ void __launch_bounds__(NT, 1)
+    k_coarse_fp32_kc(const float* __restrict__ xsT, int n, int np, int dp, int cap, int lstride,
+                     const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
+                     uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
+    constexpr int LCAP = 32 * SLOTS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* S_s = reinterpret_cast<float*>(smem_raw);            // [STAGES][KC][BM + BN]
+    float* L_s = S_s + (size_t)STAGES * KC * (BM + BN);          // [BM][LCAP]
+    uint32_t* L_i = reinterpret_cast<uint32_t*>(L_s + BM * LCAP);
+    float* buf_s = reinterpret_cast<float*>(L_i + BM * LCAP);   // [BM][BUF]
+    uint32_t* buf_i = reinterpret_cast<uint32_t*>(buf_s + BM * BUF);
+    int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);       // [BM]
+    int* len_s = cnt_s + BM;                                     // [BM]
+    float* tau_s = reinterpret_cast<float*>(len_s + BM);         // [BM]
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int q0 = blockIdx.x * BM;
+    const int nq = qlist ? min(BM, (int)*qcount - q0) : BM;
+    if (nq <= 0) return;
+    auto row_of = [&](int qi) -> int { return qlist ? (qi < nq ? (int)qlist[q0 + qi] : -1) : q0 + qi; };
+    const int all_tiles = np / BN, tps = (all_tiles + gridDim.y - 1) / gridDim.y;
+    const int tile0 = blockIdx.y * tps, ntiles = max(0, min(all_tiles, tile0 + tps) - tile0);
+    const int nch = (dp + KC - 1) / KC;
+    const int nsteps = ntiles * nch;
+
+    // Stage of step s = (tile, chunk): rows [chunk·KC, +KC) of the queries' and the tile's columns.
+    auto load_step = [&](int step) {
+        float* A = S_s + (size_t)(step % STAGES) * KC * (BM + BN);
+        float* B = A + KC * BM;
+        const int tile = tile0 + step / nch, t0 = (step % nch) * KC;
+        for (int ch = tid; ch < KC * (BM / 4); ch += NT) {
+            const int t = ch / (BM / 4), c4 = ch % (BM / 4);
+            if (t0 + t < dp) {
+                if (qlist) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int qi = c4 * 4 + u;
+                        A[t * BM + qi] = qi < nq ? xsT[(size_t)(t0 + t) * np + qlist[q0 + qi]] : 0.0f;
+                    }
+                } else {
+                    cp_async16(A + t * BM + c4 * 4, xsT + (size_t)(t0 + t) * np + q0 + c4 * 4);
+                }
+                cp_async16(B + t * BN + c4 * 4, xsT + (size_t)(t0 + t) * np + tile * BN + c4 * 4);
+            } else {
+                *reinterpret_cast<float4*>(A + t * BM + c4 * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+                *reinterpret_cast<float4*>(B + t * BN + c4 * 4) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
+    };
+    if (nsteps > 0) load_step(0);
+    cp_async_commit();
+    if (nsteps > 1) load_step(1);
+    cp_async_commit();
+    for (int q = tid; q < BM; q += NT) {
+        cnt_s[q] = 0;
+        len_s[q] = 0;
+        tau_s[q] = -CUDART_INF_F;
     }
-    for (int qi = tid; qi < BM; qi += NT) {
-        const int q = row_of(qi);
-        if (q >= 0 && q < n) tau_out[q] = tau_s[qi];
+    for (int e = tid; e < BM * LCAP; e += NT) {
+        L_s[e] = -CUDART_INF_F;
+        L_i[e] = 0u;
     }
+
+    for (int tl = 0; tl < ntiles; ++tl) {
+        const int c0 = (tile0 + tl) * BN;
+        unsigned long long acc2[8][4];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
+        for (int ch = 0; ch < nch; ++ch) {
+            const int step = tl * nch + ch;
+            cp_async_wait<1>();
+            __syncthreads();  // this step's stage landed for every thread; stage (step+2)%3 is free
+            if (step + 2 < nsteps) load_step(step + 2);
+            cp_async_commit();
+            const float* A = S_s + (size_t)(step % STAGES) * KC * (BM + BN);
+            const float* B = A + KC * BM;
+#pragma unroll 4
+            for (int t = 0; t < KC; ++t) {
+                const float4 a0 = *reinterpret_cast<const float4*>(A + t * BM + ty * 4);
+                const float4 a1 = *reinterpret_cast<const float4*>(A + t * BM + 64 + ty * 4);
+                const float4 b0 = *reinterpret_cast<const float4*>(B + t * BN + tx * 4);
+                const float4 b1 = *reinterpret_cast<const float4*>(B + t * BN + 64 + tx * 4);
+                const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const unsigned long long bp[4] = {pack2(b0.x, b0.y), pack2(b0.z, b0.w), pack2(b1.x, b1.y),
+                                                  pack2(b1.z, b1.w)};
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const unsigned long long ap = pack2(a[i], a[i]);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc2[i][j] = ffma2(ap, bp[j], acc2[i][j]);
+                }
+            }
+        }
+        float acc[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
+        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, warp, lane, tx, ty, row_of,
+                           [&](int qi, int cl) {
+                               // zero padding beyond dp adds exact zeros: the chain over dp is the same
+                               const int q = row_of(qi);
+                               float sv = 0.0f;
+                               if (q >= 0)
+                                   for (int t = 0; t < dp; ++t)
+                                       sv = fmaf(xsT[(size_t)t * np + q], xsT[(size_t)t * np + c0 + cl], sv);
+                               return sv;
+                           });
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    write_lists(L_s, L_i, tau_s, LCAP, cap, lstride, n, nq, q0, part_stride, row_of, cand_idx, cand_score, tau_out);
+}
+
+constexpr int kc_for(int slots) { return slots <= 2 ? 32 : 16; }
+
+size_t coarse_smem_bytes_kc(int slots) {
+    const size_t lcap = 32 * (size_t)slots;
+    return (size_t)STAGES * kc_for(slots) * (BM + BN) * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 + BM * 4 * 3;
+}
+
+template <int S>
+cudaError_t launch_kc(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                      const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
+                      float* tau, cudaStream_t st) {
+    constexpr int KC = kc_for(S);
+    const size_t smem = coarse_smem_bytes_kc(S);
+    cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32_kc<S, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_coarse_fp32_kc<S, KC><<<dim3(np / BM, segs), NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount,
+                                                                   part_stride, cand_idx, cand_score, tau);
+    note_launch();
+    return cudaGetLastError();
 }
 
 size_t coarse_smem_bytes(int dp, int slots) {
@@ -267,43 +441,127 @@ size_t coarse_smem_bytes(int dp, int slots) {
 
 template <int S, int D>
 cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
+                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
+                       float* tau, cudaStream_t st) {
     const size_t smem = coarse_smem_bytes(dp, S);
     cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_coarse_fp32<S, D><<<np / BM, NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score,
-                                                   tau); note_launch();
+    k_coarse_fp32<S, D><<<dim3(np / BM, segs), NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount,
+                                                               part_stride, cand_idx, cand_score, tau);
+    note_launch();
     return cudaGetLastError();
 }
 
 template <int S>
 cudaError_t dispatch_d(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
-#define COSTAL_D(D) \
-    case D: return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
+                       float* tau, cudaStream_t st) {
+#define COSTAL_D(D)                                                                                            \
+    case D:                                                                                                    \
+        return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx, \
+                                cand_score, tau, st);
     switch (dp) {
         COSTAL_D(8) COSTAL_D(16) COSTAL_D(24) COSTAL_D(32) COSTAL_D(40) COSTAL_D(48) COSTAL_D(56) COSTAL_D(64)
-        default: return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+        default:
+            return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx,
+                                    cand_score, tau, st);
     }
 #undef COSTAL_D
 }
 
+cudaError_t launch_any(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
+                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
+                       float* tau, cudaStream_t st) {
+#define COSTAL_ARGS xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx, cand_score, tau, st
+    if (dp > 64) {  // deep rows: the chunked kernel
+        switch (coarse_slots(cap)) {
+            case 1: return launch_kc<1>(COSTAL_ARGS);
+            case 2: return launch_kc<2>(COSTAL_ARGS);
+            case 4: return launch_kc<4>(COSTAL_ARGS);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (coarse_slots(cap)) {
+        case 1: return dispatch_d<1>(COSTAL_ARGS);
+        case 2: return dispatch_d<2>(COSTAL_ARGS);
+        case 4: return launch_one<4, 0>(COSTAL_ARGS);
+        default: return cudaErrorInvalidValue;
+    }
+#undef COSTAL_ARGS
+}
+
+// One warp per listed row: the union of its segments' lists (segs · cap ≤ 256 entries) sorted as
+// (score desc, index asc) keys; the best cap go to the row's candidates, and τ is the cap-th score
+// (≥ every segment's own τ, since a full segment list holds cap entries at or above it).
+__global__ void k_merge_parts(const uint32_t* __restrict__ qlist, int count, int segs, int cap,
+                              const uint32_t* __restrict__ part_idx, const float* __restrict__ part_score,
+                              int lstride, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
+                              float* __restrict__ tau_out) {
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (r >= count) return;
+    uint64_t key[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int e = s * 32 + lane;
+        key[s] = PAD_KEY;
+        if (e < segs * cap) {
+            const size_t o = ((size_t)(e / cap) * count + r) * cap + e % cap;
+            key[s] = order_key(part_score[o], part_idx[o]);
+        }
+    }
+    warp_sort_keys<8>(key, lane);
+    const uint32_t q = qlist[r];
+    uint64_t kth = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int p = s * 32 + lane;
+        if (p < cap) {
+            cand_idx[(size_t)q * lstride + p] = key_index(key[s]);
+            cand_score[(size_t)q * lstride + p] = key_score(key[s]);
+        }
+        if (s == (cap - 1) >> 5) kth = key[s];
+    }
+    const uint64_t t = __shfl_sync(COSTAL_FULL_MASK, kth, (cap - 1) & 31);
+    if (lane == 0) tau_out[q] = key_score(t);
+}
+
 }  // namespace plain
 
-size_t coarse_fp32_smem(int dp, int cap) { return plain::coarse_smem_bytes(dp, coarse_slots(cap)); }
+size_t coarse_fp32_smem(int dp, int cap) {
+    return dp > 64 ? plain::coarse_smem_bytes_kc(coarse_slots(cap)) : plain::coarse_smem_bytes(dp, coarse_slots(cap));
+}
 
 int coarse_dpad(int d) { return d <= 64 ? ((d < 1 ? 1 : d) + 7) / 8 * 8 : (d + 3) / 4 * 4; }
 
 cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
                                const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
                                cudaStream_t st) {
-    switch (coarse_slots(cap)) {
-        case 1: return plain::dispatch_d<1>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
-        case 2: return plain::dispatch_d<2>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
-        case 4:
-            return plain::launch_one<4, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
-        default: return cudaErrorInvalidValue;
-    }
+    return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, 0, cand_idx, cand_score, tau, st);
+}
+
+int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
+    const int qblocks = (count + plain::BM - 1) / plain::BM, all = np / plain::BN;
+    int segs = (2 * sm_count + qblocks - 1) / qblocks;
+    segs = std::min(segs, 256 / cap);
+    segs = std::min(segs, all / 2);
+    if (segs <= 1) return 1;
+    const int tps = (all + segs - 1) / segs;
+    return (all + tps - 1) / tps;  // no empty segment
+}
+
+cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, int cap, int lstride,
+                                     const uint32_t* qlist, const unsigned* qcount, int count, int segs,
+                                     uint32_t* part_idx, float* part_score, float* part_tau, uint32_t* cand_idx,
+                                     float* cand_score, float* tau, cudaStream_t st) {
+    if (segs <= 1) return launch_coarse_fp32(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
+    cudaError_t e = plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, count, part_idx, part_score,
+                                      part_tau, st);
+    if (e != cudaSuccess) return e;
+    plain::k_merge_parts<<<(count + 7) / 8, 256, 0, st>>>(qlist, count, segs, cap, part_idx, part_score, lstride,
+                                                          cand_idx, cand_score, tau);
+    note_launch();
+    return cudaGetLastError();
 }
 
 }  // namespace costal

@@ -113,7 +113,14 @@ __global__ void k_row_l2_norms_f32(const float* __restrict__ x, int n, int d, fl
 // k_rescore: f64 rescoring, sort, certificate, fused Tanimoto weight
 // =================================================================================================
 
+// before64 without short-circuit evaluation: a predicate, never a branch.
+__device__ __forceinline__ bool before64_p(double sa, uint32_t ia, double sb, uint32_t ib) {
+    const long long ka = total_key(sa), kb = total_key(sb);
+    return (ka > kb) | ((ka == kb) & (ia < ib));
+}
+
 // Bitonic sort of a warp-distributed array (position p = s·32 + lane) into (score desc, idx asc).
+// Every compare-exchange is a predicate and selects, so the warp never diverges between shuffles.
 template <int SLOTS>
 __device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOTS], uint32_t (&id)[SLOTS],
                                           int lane) {
@@ -129,12 +136,16 @@ __device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOT
                     const int t = s ^ ss;
                     if (t > s) {
                         const bool asc = ((s * 32 + lane) & size) == 0;
-                        const bool sw = asc ? before64(sc[t], id[t], sc[s], id[s]) : before64(sc[s], id[s], sc[t], id[t]);
-                        if (sw) {
-                            double a = sc[s]; sc[s] = sc[t]; sc[t] = a;
-                            double b = cs[s]; cs[s] = cs[t]; cs[t] = b;
-                            uint32_t c = id[s]; id[s] = id[t]; id[t] = c;
-                        }
+                        const bool sw = asc ? before64_p(sc[t], id[t], sc[s], id[s])
+                                            : before64_p(sc[s], id[s], sc[t], id[t]);
+                        const double a = sc[s], b = cs[s];
+                        const uint32_t c = id[s];
+                        sc[s] = sw ? sc[t] : a;
+                        cs[s] = sw ? cs[t] : b;
+                        id[s] = sw ? id[t] : c;
+                        sc[t] = sw ? a : sc[t];
+                        cs[t] = sw ? b : cs[t];
+                        id[t] = sw ? c : id[t];
                     }
                 }
             } else {
@@ -145,12 +156,11 @@ __device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOT
                     const uint32_t oid = __shfl_xor_sync(COSTAL_FULL_MASK, id[s], stride);
                     const bool lower = (lane & stride) == 0;
                     const bool asc = ((s * 32 + lane) & size) == 0;
-                    const bool take = (lower == asc) ? before64(osc, oid, sc[s], id[s]) : before64(sc[s], id[s], osc, oid);
-                    if (take) {
-                        sc[s] = osc;
-                        cs[s] = ocs;
-                        id[s] = oid;
-                    }
+                    const bool take = (lower == asc) ? before64_p(osc, oid, sc[s], id[s])
+                                                     : before64_p(sc[s], id[s], osc, oid);
+                    sc[s] = take ? osc : sc[s];
+                    cs[s] = take ? ocs : cs[s];
+                    id[s] = take ? oid : id[s];
                 }
             }
         }
@@ -173,6 +183,7 @@ __global__ void __launch_bounds__(256)
     const int i = rlist ? (int)rlist[w] : w;
     const double ni = norms[i];
     const float* xi = x + (size_t)i * d;
+    const bool vec4 = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
     double sc[SLOTS], cs[SLOTS];
     uint32_t id[SLOTS];
     double err = 0.0;
@@ -184,7 +195,18 @@ __global__ void __launch_bounds__(256)
             // (an index ≥ n marks an empty slot: the coarse pass kept fewer than cap candidates)
             const float* xj = x + (size_t)j * d;
             double dot = 0.0;
-            for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
+            if (vec4) {  // the same dimension order, 16-byte loads
+                for (int t = 0; t < d; t += 4) {
+                    const float4 a = __ldg(reinterpret_cast<const float4*>(xi + t));
+                    const float4 b = __ldg(reinterpret_cast<const float4*>(xj + t));
+                    dot = dot64_step(dot, a.x, b.x);
+                    dot = dot64_step(dot, a.y, b.y);
+                    dot = dot64_step(dot, a.z, b.z);
+                    dot = dot64_step(dot, a.w, b.w);
+                }
+            } else {
+                for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
+            }
             const double nj = norms[j];
             const double c = cos64(dot, ni, nj);
             const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
@@ -200,7 +222,11 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
-    if (lane == 0 && max_err_bits) atomicMax(max_err_bits, (unsigned long long)__double_as_longlong(err));
+    // one address for the whole grid: read it first, so that only a new maximum pays for the atomic
+    if (lane == 0 && max_err_bits) {
+        const unsigned long long eb = (unsigned long long)__double_as_longlong(err);
+        if (eb > *reinterpret_cast<volatile unsigned long long*>(max_err_bits)) atomicMax(max_err_bits, eb);
+    }
     warp_sort<SLOTS>(sc, cs, id, lane);
     const double s_k = __shfl_sync(COSTAL_FULL_MASK, sc[(k - 1) >> 5], (k - 1) & 31);
     const double e = row_eps ? row_eps[i] : eps;

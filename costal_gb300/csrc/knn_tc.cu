@@ -15,8 +15,8 @@
 //             accumulators; warps 0-3 read the accumulators back (tcgen05.ld, 64 columns at a time,
 //             the next load in flight while one is scanned), reject whole slices with a 3-input max
 //             tree against the query's threshold, and append the rare survivors to per-query buffers
-//             that the warp flushes cooperatively into sorted per-query lists in shared memory
-//             (score desc, index asc; strict `v > τ` admission, knn.rs:774-780).
+//             that the warp shrinks cooperatively to the best cap (strict `v > τ` admission,
+//             knn.rs:774-780).
 //   bound     Every query row i gets a rigorous bound E_i on |coarse − exact cosine| (k_row_eps):
 //             split remainder ‖a_lo‖·max‖b_lo‖ + ‖a_hi+a_lo‖·max‖r_b‖ + ‖r_a‖·max‖b_hi+b_lo‖ + ‖r_a‖·max‖r_b‖
 //             (Cauchy–Schwarz), plus the tensor-core accumulation (K + 16)·2⁻²¹·Σ|products| (four
@@ -187,49 +187,101 @@ struct __align__(8) Barriers {
 // Per-query candidate buffer: BCAP = 2·LCAP entries in shared memory, [entry][query] with a row
 // stride of BLOCK_M + 1 words (appends of 32 lanes and the warp's reads of one query are both free
 // of bank conflicts). Survivors are appended with predicated stores; when a buffer could overflow,
-// the warp sorts it cooperatively, keeps the best `cap` and raises τ to the cap-th score. Every
-// candidate outside a buffer scored ≤ τ when it was seen or evicted, and τ only grows.
+// the warp selects its best `cap` cooperatively (radix select, no sort) and raises τ to the cap-th
+// score. Every candidate outside a buffer scored ≤ τ when it was seen or evicted, and τ only grows.
 constexpr int BSTRIDE = BLOCK_M + 1;
 
-// Sort one query's buffer (cntL entries) and keep its best `cap` entries at positions 0..cap-1.
+// f32 score → u32 with the same order (every admitted score is finite).
+__device__ __forceinline__ uint32_t fkey(float v) {
+    const uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Shrink one query's buffer (cntL entries, all above its threshold tauL) to `cap` entries and return
+// the new threshold: T = the cap-th largest score, found by a warp-wide radix select on the order
+// keys (bit by bit from the highest bit where the buffer's keys differ, one ballot per slot a bit);
+// the entries above T and enough of those equal to T are compacted to positions 0..cap-1 in buffer
+// order. Entries dropped score ≤ T, so "everything outside the buffer scores ≤ τ" still holds. With
+// cntL ≤ cap nothing changes.
 template <int SL>
-__device__ __noinline__ void flush_one(float* B_s, uint32_t* B_i, int qL, int cntL, int cap, int lane, float* tau_out) {
-    uint64_t key[SL];
+__device__ __noinline__ float flush_one(float* B_s, uint32_t* B_i, int qL, int cntL, int cap, int lane, float tauL) {
+    if (cntL <= cap) return tauL;
+    float sc[SL];
+    uint32_t id[SL], key[SL];
+    uint32_t kmin = 0xffffffffu, kmax = 0u;
 #pragma unroll
     for (int s = 0; s < SL; ++s) {
         const int p = s * 32 + lane;
-        key[s] = p < cntL ? order_key(B_s[p * BSTRIDE + qL], B_i[p * BSTRIDE + qL]) : PAD_KEY;
-    }
-    warp_sort_keys<SL>(key, lane);
-    uint64_t kth = 0;
-#pragma unroll
-    for (int s = 0; s < SL; ++s) {
-        const int p = s * 32 + lane;
-        if (p < cap) {
-            B_s[p * BSTRIDE + qL] = key_score(key[s]);
-            B_i[p * BSTRIDE + qL] = key_index(key[s]);
+        const bool v = p < cntL;
+        sc[s] = v ? B_s[p * BSTRIDE + qL] : 0.0f;
+        id[s] = v ? B_i[p * BSTRIDE + qL] : 0u;
+        key[s] = v ? fkey(sc[s]) : 0u;  // 0: below every valid key
+        if (v) {
+            kmin = min(kmin, key[s]);
+            kmax = max(kmax, key[s]);
         }
-        if (s == (cap - 1) >> 5) kth = key[s];
     }
-    const float t = key_score(__shfl_sync(COSTAL_FULL_MASK, kth, (cap - 1) & 31));
-    if (lane == 0) *tau_out = t;
+    kmin = __reduce_min_sync(COSTAL_FULL_MASK, kmin);
+    kmax = __reduce_max_sync(COSTAL_FULL_MASK, kmax);
+    // T lies in [kmin, kmax]: its bits above the highest differing bit are theirs
+    const uint32_t diff = kmin ^ kmax;
+    const int top = diff ? 31 - __clz(diff) : -1;
+    uint32_t T = top >= 0 ? (kmax & ~((2u << top) - 1u)) : kmax;
+    for (int b = top; b >= 0; --b) {
+        const uint32_t c = T | (1u << b);
+        int n_ge = 0;
+#pragma unroll
+        for (int s = 0; s < SL; ++s) n_ge += __popc(__ballot_sync(COSTAL_FULL_MASK, key[s] >= c));
+        if (n_ge >= cap) T = c;
+    }
+    // keep key > T, and the first (cap − #{key > T}) entries with key == T
+    int n_gt = 0;
+#pragma unroll
+    for (int s = 0; s < SL; ++s) n_gt += __popc(__ballot_sync(COSTAL_FULL_MASK, key[s] > T));
+    const unsigned below = (1u << lane) - 1u;
+    int eq_before = 0, kept_before = 0;
+    bool keep[SL];
+    int pos[SL];
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+        const unsigned meq = __ballot_sync(COSTAL_FULL_MASK, key[s] == T);
+        const bool k = key[s] > T || (key[s] == T && eq_before + __popc(meq & below) < cap - n_gt);
+        const unsigned mk = __ballot_sync(COSTAL_FULL_MASK, k);
+        keep[s] = k;
+        pos[s] = kept_before + __popc(mk & below);
+        eq_before += __popc(meq);
+        kept_before += __popc(mk);
+    }
+    __syncwarp();  // every lane has read its entries before any is overwritten
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+        if (keep[s]) {
+            B_s[pos[s] * BSTRIDE + qL] = sc[s];
+            B_i[pos[s] * BSTRIDE + qL] = id[s];
+        }
+    }
     __syncwarp();
+    return fkey_inv(T);
 }
 
 // Flush every lane whose buffer holds more than `limit` entries.
 template <int SL>
-__device__ __forceinline__ void flush_full(float* B_s, uint32_t* B_i, float* tau_s, int qbase, int lane, int cap,
-                                           int limit, int& cnt, float& tau) {
+__device__ __forceinline__ void flush_full(float* B_s, uint32_t* B_i, int qbase, int lane, int cap, int limit, int& cnt,
+                                           float& tau) {
     unsigned pend = __ballot_sync(COSTAL_FULL_MASK, cnt > limit);
     if (!pend) return;
     __syncwarp();  // the lanes' appends are visible to the whole warp
     while (pend) {
         const int L = __ffs(pend) - 1;
         pend &= pend - 1;
-        flush_one<SL>(B_s, B_i, qbase + L, __shfl_sync(COSTAL_FULL_MASK, cnt, L), cap, lane, &tau_s[qbase + L]);
+        const float t = flush_one<SL>(B_s, B_i, qbase + L, __shfl_sync(COSTAL_FULL_MASK, cnt, L), cap, lane,
+                                      __shfl_sync(COSTAL_FULL_MASK, tau, L));
         if (lane == L) {
             cnt = min(cnt, cap);
-            tau = tau_s[qbase + L];
+            tau = t;
         }
     }
 }
@@ -285,7 +337,7 @@ __device__ __forceinline__ unsigned slice_mask(const uint32_t (&r)[64], float ta
 // itself). Kept out of line: the rare path stays off the hot loop's instruction footprint.
 template <int SL>
 __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb, int n, int q, int qi, int qbase,
-                                          int lane, int cap, int q_lo, float* B_s, uint32_t* B_i, float* tau_s,
+                                          int lane, int cap, int q_lo, float* B_s, uint32_t* B_i,
                                           int* cnt_io, float* tau_io) {
     constexpr int BCAP = 32 * SL;
     int cnt = *cnt_io;
@@ -306,7 +358,7 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
                 ++cnt;
             }
         }
-        flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, BCAP - 8, cnt, tau);
+        flush_full<SL>(B_s, B_i, qbase, lane, cap, BCAP - 8, cnt, tau);
     }
     *cnt_io = cnt;
     *tau_io = tau;
@@ -330,8 +382,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     unsigned char* b_tiles = a_tile + (size_t)nkb * A_KB_BYTES;     // stages × nkb × 32 KB
     float* B_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * nkb * B_KB_BYTES);  // [BCAP][BSTRIDE]
     uint32_t* B_i = reinterpret_cast<uint32_t*>(B_s + BCAP * BSTRIDE);
-    float* tau_s = reinterpret_cast<float*>(B_i + BCAP * BSTRIDE);  // [128] flush results
-    Barriers* bars = reinterpret_cast<Barriers*>(tau_s + BLOCK_M);
+    Barriers* bars = reinterpret_cast<Barriers*>(B_i + BCAP * BSTRIDE);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Rows and columns are in the working order (rows sorted by locality cell; perm maps back to the
@@ -377,6 +428,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int s = t % stages;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u;
                 if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) break;
+                if ((unsigned)block_of(t) >= (unsigned)(np / BLOCK_N)) {
+                    // a list entry outside the operands (never produced by the list kernel): report it
+                    // and stop the CTA here like an early stop, so no role reads past the operands
+                    atomicExch(timeout_flag, 2ull);
+                    *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
+                    mbar_arrive(&bars->b_full[s]);
+                    break;
+                }
                 if (t > 0 && my_ub) {
                     // Every column of list entry t (and of all later ones: the bounds do not increase)
                     // has cosine ≤ my_ub[t]; its coarse score is ≤ my_ub[t] + E_i. When that is below
@@ -473,7 +532,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     cnt_m = cnt;
                     tau_m = tau;
                     admit_groups<SL>(gm, tb + (uint32_t)(128 * h), c0 + 128 * h, n, q, qi, qbase, lane, cap, q_lo, B_s,
-                                     B_i, tau_s, &cnt_m, &tau_m);
+                                     B_i, &cnt_m, &tau_m);
                     cnt = cnt_m;
                     tau = tau_m;
                 }
@@ -484,7 +543,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     cnt_m = cnt;
                     tau_m = tau;
                     admit_groups<SL>(gm, tb + (uint32_t)(128 * h + 64), c0 + 128 * h + 64, n, q, qi, qbase, lane, cap,
-                                     q_lo, B_s, B_i, tau_s, &cnt_m, &tau_m);
+                                     q_lo, B_s, B_i, &cnt_m, &tau_m);
                     cnt = cnt_m;
                     tau = tau_m;
                 }
@@ -504,8 +563,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         __int_as_float(key >= 0 ? key : key ^ 0x7fffffff);
             }
         }
-        // final selection: every buffer sorted, best `cap` first
-        flush_full<SL>(B_s, B_i, tau_s, qbase, lane, cap, 0, cnt, tau);
+        // final selection: every buffer down to its best `cap` entries (in buffer order)
+        flush_full<SL>(B_s, B_i, qbase, lane, cap, cap, cnt, tau);
         __syncwarp();
         if (q < n) {
             const uint32_t qo = perm ? perm[q] : (uint32_t)q;
@@ -528,20 +587,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 // ---- operand preparation ----------------------------------------------------------------------
 
-// One thread per padded row: split the normalised row (read from xsT) into the two operands and
-// record the f64 norms of its pieces: [0] ‖a_hi‖, [1] ‖a_lo‖, [2] ‖r‖, [3] ‖a_hi + a_lo‖.
-__global__ void k_split(const float* __restrict__ xsT, int n, int np, int d, int kp, const uint32_t* __restrict__ perm,
-                        __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
-                        unsigned long long* __restrict__ colmax) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;  // working row
-    if (r >= np) return;
-    const int o = r < n ? (perm ? (int)perm[r] : r) : 0;  // its original row
-    __nv_bfloat16* ra = opa + (size_t)r * kp;
-    __nv_bfloat16* rb = opb + (size_t)r * kp;
+// One CTA per 128 working rows: each thread splits its row (read from xsT at the original index)
+// into the two operands in shared memory and records the f64 norms of the pieces: [0] ‖a_hi‖,
+// [1] ‖a_lo‖, [2] ‖r‖, [3] ‖a_hi + a_lo‖; then the CTA writes the 128 operand rows with coalesced
+// word stores. Rows in [n, rows) are written as zeros. The maxima over rows go to colmax through one
+// atomic per warp.
+constexpr int SPLIT_ROWS = 128;
+__global__ void __launch_bounds__(SPLIT_ROWS)
+    k_split(const float* __restrict__ xsT, int n, int np_x, int rows, int d, int kp, const uint32_t* __restrict__ perm,
+            __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
+            unsigned long long* __restrict__ colmax) {
+    extern __shared__ uint32_t sw[];  // [2][SPLIT_ROWS][kp/2 + 1] words of bf16 pairs
+    const int ws = kp / 2 + 1;        // odd word stride: the 32 lanes' rows fall in 32 banks
+    __nv_bfloat16* ta = reinterpret_cast<__nv_bfloat16*>(sw);
+    __nv_bfloat16* tb = reinterpret_cast<__nv_bfloat16*>(sw + SPLIT_ROWS * ws);
+    const int lr = threadIdx.x, r = blockIdx.x * SPLIT_ROWS + lr;  // working row
+    const bool live = r < n;
+    const int o = live ? (perm ? (int)perm[r] : r) : 0;  // its original row
+    __nv_bfloat16* ra = ta + (size_t)lr * 2 * ws;
+    __nv_bfloat16* rb = tb + (size_t)lr * 2 * ws;
     double sh = 0.0, sl = 0.0, sr = 0.0, sp = 0.0;
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
     for (int t = 0; t < d; ++t) {
-        const float a = r < n ? xsT[(size_t)t * np + o] : 0.0f;
+        const float a = live ? xsT[(size_t)t * np_x + o] : 0.0f;
         const __nv_bfloat16 hb = __float2bfloat16_rn(a);
         const float h = __bfloat162float(hb);
         const float e = a - h;  // exact in f32
@@ -564,11 +632,29 @@ __global__ void k_split(const float* __restrict__ xsT, int n, int np, int d, int
         ra[t] = zero;
         rb[t] = zero;
     }
-    if (r < n) {
-        const double v[4] = {sqrt(sh), sqrt(sl), sqrt(sr), sqrt(sp)};
-        for (int j = 0; j < 4; ++j) {
-            pnorm[(size_t)j * n + o] = v[j];
-            atomicMax(&colmax[j], (unsigned long long)__double_as_longlong(v[j]));
+    const double v[4] = {sqrt(sh), sqrt(sl), sqrt(sr), sqrt(sp)};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (live) pnorm[(size_t)j * n + o] = v[j];
+        // non-negative doubles order like their bit patterns
+        unsigned long long b = live ? (unsigned long long)__double_as_longlong(v[j]) : 0ull;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long ob = __shfl_xor_sync(COSTAL_FULL_MASK, b, off);
+            b = ob > b ? ob : b;
+        }
+        if ((threadIdx.x & 31) == 0 && b > *reinterpret_cast<volatile unsigned long long*>(&colmax[j]))
+            atomicMax(&colmax[j], b);
+    }
+    __syncthreads();
+    const int wpr = kp / 2;  // words per operand row
+    uint32_t* ga = reinterpret_cast<uint32_t*>(opa) + (size_t)blockIdx.x * SPLIT_ROWS * wpr;
+    uint32_t* gb = reinterpret_cast<uint32_t*>(opb) + (size_t)blockIdx.x * SPLIT_ROWS * wpr;
+    for (int e = threadIdx.x; e < SPLIT_ROWS * wpr; e += SPLIT_ROWS) {
+        const int row = e / wpr, w = e % wpr;
+        if (blockIdx.x * SPLIT_ROWS + row < rows) {
+            ga[e] = sw[row * ws + w];
+            gb[e] = sw[SPLIT_ROWS * ws + row * ws + w];
         }
     }
 }
@@ -595,7 +681,7 @@ static int kpad(int d) { return (3 * d + KB - 1) / KB * KB; }
 
 static size_t fixed_smem(int nkb, int cap) {
     const int bcap = cap <= 32 ? 64 : 128;
-    return 1024 + (size_t)nkb * A_KB_BYTES + (size_t)(BLOCK_M + 1) * bcap * 8 + (size_t)BLOCK_M * 4 + sizeof(Barriers);
+    return 1024 + (size_t)nkb * A_KB_BYTES + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
 }
 
 bool supported(int d, int cap) {
@@ -666,8 +752,13 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     Layout L = carve(ws, n, d);
     cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
     if (e != cudaSuccess) return e;
-    // xsT has n_pad = ⌈n/128⌉·128 columns; rows in [n, np) are zero-filled by k_split itself.
-    k_split<<<(np + 127) / 128, 128, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax); note_launch();
+    // xsT has ⌈n/128⌉·128 columns; operand rows in [n, np) are zero-filled by k_split itself.
+    const size_t smem = (size_t)2 * SPLIT_ROWS * (kp / 2 + 1) * 4;
+    e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, kp, perm, L.opa, L.opb, L.pnorm,
+                                                        L.colmax);
+    note_launch();
     k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps); note_launch();
     plan.n = n;
     plan.d = d;
@@ -708,3 +799,4 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
 
 }  // namespace tc
 }  // namespace costal
+

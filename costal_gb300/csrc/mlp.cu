@@ -49,32 +49,34 @@ __global__ void k_features(const float* __restrict__ xsT, int np, int d, const f
     for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[(e / d) * ds + e % d] = cent[e];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (i >= m) return;
-    const uint32_t r = rows ? rows[i] : (uint32_t)i;
     const int F = d + MLP_TOPC;
-    float dot[8];
+    const int wpb = blockDim.x >> 5;
+    // grid-stride over rows, one warp per row: the centroids are loaded once per CTA
+    for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
+        const uint32_t r = rows ? rows[i] : (uint32_t)i;
+        float dot[8];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
-    for (int t = 0; t < d; ++t) {
-        const float a = xsT[(size_t)t * np + r];
+        for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
+        for (int t = 0; t < d; ++t) {
+            const float a = xsT[(size_t)t * np + r];
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int c = s * 32 + lane;
+                if (c < K) dot[s] = fmaf(a, c_s[c * ds + t], dot[s]);
+            }
+        }
+        uint64_t key[8];
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
             const int c = s * 32 + lane;
-            if (c < K) dot[s] = fmaf(a, c_s[c * ds + t], dot[s]);
+            key[s] = c < K ? order_key(dot[s], (uint32_t)c) : PAD_KEY;
         }
+        warp_sort_keys<8>(key, lane);
+        float* f = feat + (size_t)i * F;
+        for (int t = lane; t < d; t += 32) f[t] = xsT[(size_t)t * np + r];
+        f[d + lane] = key_score(key[0]);
+        f[d + 32 + lane] = key_score(key[1]);
     }
-    uint64_t key[8];
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const int c = s * 32 + lane;
-        key[s] = c < K ? order_key(dot[s], (uint32_t)c) : PAD_KEY;
-    }
-    warp_sort_keys<8>(key, lane);
-    float* f = feat + (size_t)i * F;
-    for (int t = lane; t < d; t += 32) f[t] = xsT[(size_t)t * np + r];
-    f[d + lane] = key_score(key[0]);
-    f[d + 32 + lane] = key_score(key[1]);
 }
 
 // ---- forward (shared by inference and training) ------------------------------------------------
@@ -342,7 +344,11 @@ cudaError_t features(const float* xsT, int np, int d, const float* centroids, in
     const size_t smem = (size_t)K * (d | 1) * 4;
     cudaError_t e = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_features<<<(m + 7) / 8, 256, smem, st>>>(xsT, np, d, centroids, K, rows, m, feat); note_launch();
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int blocks = (m + 7) / 8 < 4 * sms ? (m + 7) / 8 : 4 * sms;
+    k_features<<<blocks, 256, smem, st>>>(xsT, np, d, centroids, K, rows, m, feat); note_launch();
     return cudaGetLastError();
 }
 

@@ -12,8 +12,9 @@
 //             unit centre c and an angular radius r = max angle(row, c), in f64;
 //   bound     for q ∈ Q, x ∈ B: angle(q, x) ≥ angle(c_Q, c_B) − r_Q − r_B (the angle is a metric on
 //             the sphere), so cos(q, x) ≤ UB(Q, B) = cos(max(0, angle(c_Q, c_B) − r_Q − r_B − ξ)),
-//             with ξ = 1e-6 rad covering the f32 rounding of the normalised rows (≤ 1e-7 rad) and the
-//             f64 evaluation;
+//             with ξ = 1e-6 rad covering the f32 rounding of the normalised rows (≤ 1e-7 rad); UB is
+//             evaluated in f32 with directed roundings and margins for the f32 dot, acosf and cosf
+//             (block_ub_f32), so it stays an upper bound;
 //   lists     for every Q, the column blocks with UB ≥ t_Q, sorted by UB descending (the closest
 //             blocks first, so a query's threshold rises to its final value within the first tiles),
 //             and ub_skip[Q] = the largest UB of a skipped block. A query is certified only if its
@@ -177,7 +178,8 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell, int n, int K, 
 // One CTA per block of `bs` consecutive working rows: centre = normalised f64 sum (row order),
 // radius = the largest angle between a row and the centre (f64). Rows past n are ignored.
 __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const uint32_t* __restrict__ perm, int n,
-                             int bs, double* __restrict__ center, double* __restrict__ radius) {
+                             int bs, double* __restrict__ center, double* __restrict__ radius,
+                             float* __restrict__ center_f, float* __restrict__ radius_f) {
     __shared__ double c_s[64];
     __shared__ double red[256];
     const int b = blockIdx.x;
@@ -195,7 +197,10 @@ __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const
         for (int t = 0; t < d; ++t) c_s[t] *= inv;
     }
     __syncthreads();
-    if (threadIdx.x < d) center[(size_t)b * d + threadIdx.x] = c_s[threadIdx.x];
+    if (threadIdx.x < d) {
+        center[(size_t)b * d + threadIdx.x] = c_s[threadIdx.x];
+        if (center_f) center_f[(size_t)threadIdx.x * gridDim.x + b] = (float)c_s[threadIdx.x];  // [d][blocks]
+    }
     double worst = 0.0;
     for (int w = r0 + threadIdx.x; w < r1; w += blockDim.x) {
         const uint32_t o = perm[w];
@@ -215,108 +220,173 @@ __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const
         if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) radius[b] = red[0];
+    if (threadIdx.x == 0) {
+        radius[b] = red[0];
+        if (radius_f) {
+            float rf = (float)red[0];
+            if ((double)rf < red[0]) rf = nextafterf(rf, CUDART_INF_F);  // rounded up
+            radius_f[b] = rf;
+        }
+    }
 }
 
 // ---- per-query-block lists ------------------------------------------------------------------------
 
 constexpr int LIST_T = 512;
+constexpr int LIST_KPT = 16;                 // list entries per thread
+constexpr int LIST_N = LIST_T * LIST_KPT;    // 8192: the most column blocks a list is sorted for
 constexpr double XI = 1e-6;
 
-__device__ __forceinline__ double block_ub(const double* cq, double rq, const double* cb, double rb, int d) {
-    double dot = 0.0;
-    for (int t = 0; t < d; ++t) dot += cq[t] * cb[t];
-    const double phi = acos(fmin(1.0, fmax(-1.0, dot)));
-    const double th = fmax(0.0, phi - rq - rb - XI);
-    return cos(th);
+// The bound in f32 for one (query block, column block) pair, rigorous for the f64 geometry: the
+// f32 FMA dot of the two unit centres (each rounded to f32) is within (d + 2)·2⁻²⁴ of the f64 value,
+// so acos(dot + δ) with δ = (d + 4)·2⁻²³, the sum rounded up, never exceeds the centres' angle;
+// acosf and cosf are within a few ulp, covered by 1e-6 on each side; every subtraction rounds down
+// and the final addition up. Radii arrive rounded up to f32.
+__device__ __forceinline__ float block_ub_f32(const float* cq, float rq, const float* cb, int cstride, float rb, int d) {
+    float dot = 0.0f;
+    for (int t = 0; t < d; ++t) dot = fmaf(cq[t], cb[(size_t)t * cstride], dot);
+    const float delta = (float)(d + 4) * 0x1p-23f;
+    const float c = fminf(1.0f, __fadd_ru(dot, delta));
+    const float phi = __fsub_rd(acosf(c), 1e-6f);
+    const float th = __fsub_rd(__fsub_rd(__fsub_rd(phi, rq), rb), (float)XI);
+    if (th <= 0.0f) return 1.0f;
+    return fminf(1.0f, __fadd_ru(cosf(th), 1e-6f));
 }
 
-// One CTA per query block: the upper bound against every column block, the blocks kept (UB ≥ t_Q)
-// sorted by UB descending with their bounds (shared-memory bitonic sort when they fit, else in block
-// order with bounds +inf), and the largest UB of a skipped block.
+// Compare-exchange of list keys (descending) at a register distance S within a thread's run.
+template <int S>
+__device__ __forceinline__ void cx_regs(uint64_t (&v)[LIST_KPT], int base, int size) {
+#pragma unroll
+    for (int j = 0; j < LIST_KPT; ++j) {
+        const int p = j ^ S;
+        if (p > j) {
+            const bool desc = ((base + j) & size) == 0;
+            const uint64_t a = v[j], b = v[p];
+            const uint64_t hi = a > b ? a : b, lo = a > b ? b : a;
+            v[j] = desc ? hi : lo;
+            v[p] = desc ? lo : hi;
+        }
+    }
+}
+
+// One CTA per query block: the upper bound against every column block; the blocks kept (UB ≥ t_Q)
+// sorted by (UB desc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
+// exchanged in registers, by warp shuffles or through shared memory by distance — and the largest UB
+// of a skipped block. Lists longer than LIST_N stay in block order with bounds +inf.
 __global__ void __launch_bounds__(LIST_T)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
-                  const double* __restrict__ ccenter, const double* __restrict__ cradius, int nqb, int ncb, int d,
+                  const float* __restrict__ ccenter_f, const float* __restrict__ cradius_f, int nqb, int ncb, int d,
                   const float* __restrict__ tq, uint32_t* __restrict__ lists, float* __restrict__ list_ub,
                   uint32_t* __restrict__ counts, float* __restrict__ ub_skip,
                   unsigned long long* __restrict__ skipped_total) {
-    extern __shared__ unsigned char sm[];
-    float* key = reinterpret_cast<float*>(sm);              // [8192]
-    uint32_t* id = reinterpret_cast<uint32_t*>(key + 8192);  // [8192]
-    __shared__ double cq[64];
+    extern __shared__ uint64_t xk[];  // [LIST_N] exchange buffer
+    __shared__ float cq[64];
     __shared__ unsigned kept;
     __shared__ int skip_max_bits;
-    const int Q = blockIdx.x;
-    if (threadIdx.x < d) cq[threadIdx.x] = qcenter[(size_t)Q * d + threadIdx.x];
-    if (threadIdx.x == 0) {
+    const int Q = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    if (tid < d) cq[tid] = (float)qcenter[(size_t)Q * d + tid];
+    if (tid == 0) {
         kept = 0;
         skip_max_bits = __float_as_int(-CUDART_INF_F);
     }
     __syncthreads();
-    const double rq = qradius[Q];
+    float rq = (float)qradius[Q];
+    if ((double)rq < qradius[Q]) rq = nextafterf(rq, CUDART_INF_F);
     const float t = tq ? tq[Q] : -CUDART_INF_F;
-    const bool sortable = ncb <= 8192;
     uint32_t* out = lists + (size_t)Q * ncb;
     float* out_ub = list_ub + (size_t)Q * ncb;
-    for (int b = threadIdx.x; b < ncb; b += blockDim.x) {
-        const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
-        float ubf = (float)ub;
-        if ((double)ubf < ub) ubf = nextafterf(ubf, CUDART_INF_F);  // round the bound up
-        const bool keep = ubf >= t;
-        if (keep) atomicAdd(&kept, 1u);
-        // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
-        else atomicMax(&skip_max_bits, __float_as_int(fmaxf(ubf, 0.0f)));
-        if (sortable) {
-            key[b] = keep ? ubf : -CUDART_INF_F;
-            id[b] = keep ? (uint32_t)b : 0xffffffffu;
-        }
-    }
-    __syncthreads();
-    if (sortable) {
-        int np2 = 1;
-        while (np2 < ncb) np2 <<= 1;
-        for (int b = ncb + threadIdx.x; b < np2; b += blockDim.x) {
-            key[b] = -CUDART_INF_F;
-            id[b] = 0xffffffffu;
-        }
-        __syncthreads();
-        // bitonic sort into (bound desc, block id asc); dropped blocks (−∞, id max) go last
-        for (int size = 2; size <= np2; size <<= 1) {
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                for (int e = threadIdx.x; e < np2 / 2; e += blockDim.x) {
-                    const int lo = 2 * e - (e & (stride - 1)), hi = lo + stride;
-                    const bool hi_before = key[hi] > key[lo] || (key[hi] == key[lo] && id[hi] < id[lo]);
-                    const bool lo_before = key[lo] > key[hi] || (key[lo] == key[hi] && id[lo] < id[hi]);
-                    if ((lo & size) == 0 ? hi_before : lo_before) {
-                        const float a = key[lo];
-                        key[lo] = key[hi];
-                        key[hi] = a;
-                        const uint32_t c = id[lo];
-                        id[lo] = id[hi];
-                        id[hi] = c;
-                    }
+    if (ncb > LIST_N) {
+        if (tid == 0) {
+            unsigned c = 0;
+            for (int b = 0; b < ncb; ++b) {
+                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d);
+                if (u >= t) {
+                    out_ub[c] = CUDART_INF_F;  // block order: the bounds do not decrease along the list
+                    out[c++] = (uint32_t)b;
+                } else {
+                    skip_max_bits = max(skip_max_bits, __float_as_int(fmaxf(u, 0.0f)));
                 }
-                __syncthreads();
+            }
+            kept = c;
+        }
+    } else {
+        const int base = tid * LIST_KPT;
+        uint64_t v[LIST_KPT];
+        unsigned my_kept = 0;
+        int my_skip = __float_as_int(-CUDART_INF_F);
+        // keys are computed for blocks j·LIST_T + tid (coalesced reads of the transposed centres); the
+        // sort does not care where each key starts
+#pragma unroll
+        for (int j = 0; j < LIST_KPT; ++j) {
+            const int b = j * LIST_T + tid;
+            v[j] = 0ull;  // absent or skipped: sorts last
+            if (b < ncb) {
+                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d);
+                if (u >= t) {
+                    ++my_kept;
+                    // the bound (possibly negative) as an order-preserving u32 above the complemented id
+                    const uint32_t ub = __float_as_uint(u);
+                    const uint32_t hk = (ub & 0x80000000u) ? ~ub : (ub | 0x80000000u);
+                    v[j] = ((uint64_t)hk << 32) | (uint64_t)(~(uint32_t)b);
+                } else {
+                    // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
+                    my_skip = max(my_skip, __float_as_int(fmaxf(u, 0.0f)));
+                }
             }
         }
-        for (unsigned b = threadIdx.x; b < kept; b += blockDim.x) {
-            out[b] = id[b];
-            out_ub[b] = key[b];
+        atomicAdd(&kept, my_kept);
+        atomicMax(&skip_max_bits, my_skip);
+        // the keys start interleaved over all LIST_N positions, so the sort always covers all of them
+        for (int size = 2; size <= LIST_N; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                if (stride >= LIST_KPT * 32) {  // across warps
+                    __syncthreads();
+#pragma unroll
+                    for (int j = 0; j < LIST_KPT; ++j) xk[base + j] = v[j];
+                    __syncthreads();
+#pragma unroll
+                    for (int j = 0; j < LIST_KPT; ++j) {
+                        const int e = base + j;
+                        const uint64_t o = xk[e ^ stride];
+                        const bool keep_max = ((e & stride) == 0) == ((e & size) == 0);
+                        const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                        v[j] = keep_max ? hi : lo;
+                    }
+                } else if (stride >= LIST_KPT) {  // within the warp
+                    const int lstride = stride / LIST_KPT;
+#pragma unroll
+                    for (int j = 0; j < LIST_KPT; ++j) {
+                        const int e = base + j;
+                        const uint64_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[j], lstride);
+                        const bool keep_max = ((lane & lstride) == 0) == ((e & size) == 0);
+                        const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                        v[j] = keep_max ? hi : lo;
+                    }
+                } else if (stride == 8) {
+                    cx_regs<8>(v, base, size);
+                } else if (stride == 4) {
+                    cx_regs<4>(v, base, size);
+                } else if (stride == 2) {
+                    cx_regs<2>(v, base, size);
+                } else {
+                    cx_regs<1>(v, base, size);
+                }
+            }
         }
-    } else if (threadIdx.x == 0) {
-        unsigned c = 0;
-        for (int b = 0; b < ncb; ++b) {
-            const double ub = block_ub(cq, rq, ccenter + (size_t)b * d, cradius[b], d);
-            float ubf = (float)ub;
-            if ((double)ubf < ub) ubf = nextafterf(ubf, CUDART_INF_F);
-            if (ubf >= t) {
-                out_ub[c] = CUDART_INF_F;  // block order: the bounds do not decrease along the list
-                out[c++] = (uint32_t)b;
+        __syncthreads();  // kept is final
+        const unsigned nk = kept;
+#pragma unroll
+        for (int j = 0; j < LIST_KPT; ++j) {
+            const unsigned e = (unsigned)(base + j);
+            if (e < nk) {
+                const uint32_t hk = (uint32_t)(v[j] >> 32);
+                out[e] = ~(uint32_t)v[j];
+                out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
             }
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         counts[Q] = kept;
         ub_skip[Q] = __int_as_float(skip_max_bits);
         if (skipped_total) atomicAdd(skipped_total, (unsigned long long)(ncb - (int)kept));
@@ -348,8 +418,8 @@ size_t workspace_bytes(int n, int d) {
     const size_t nqb = (size_t)(n + QB - 1) / QB, ncb = (size_t)(n + CB - 1) / CB;
     const size_t m = (size_t)(n < SAMPLE ? n : SAMPLE), nch = (size_t)(n + CHUNK - 1) / CHUNK;
     return a256(n * 4ull) * 2 + a256((size_t)K_CENTROIDS * d * 4) + a256(nqb * d * 8) + a256(nqb * 8) +
-           a256(ncb * d * 8) + a256(ncb * 8) + 2 * a256(nqb * ncb * 4) + a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) +
-           a256(nqb * 4) + a256(m * d * 4) + a256(m * 4) + a256(nch * K_CENTROIDS * 4) + a256((K_CENTROIDS + 1) * 4) +
+           a256(ncb * d * 8) + a256(ncb * 8) + a256(ncb * d * 4) + a256(ncb * 4) + 2 * a256(nqb * ncb * 4) +
+           a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) + a256(nqb * 4) + a256(m * d * 4) + a256(m * 4) + a256(nch * K_CENTROIDS * 4) + a256((K_CENTROIDS + 1) * 4) +
            a256(m * 4) + 4096;
 }
 
@@ -399,6 +469,8 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     P.qradius = reinterpret_cast<double*>(take((size_t)nqb * 8));
     P.ccenter = reinterpret_cast<double*>(take((size_t)ncb * d * 8));
     P.cradius = reinterpret_cast<double*>(take((size_t)ncb * 8));
+    P.ccenter_f = reinterpret_cast<float*>(take((size_t)ncb * d * 4));
+    P.cradius_f = reinterpret_cast<float*>(take((size_t)ncb * 4));
     P.lists = reinterpret_cast<uint32_t*>(take((size_t)nqb * ncb * 4));
     P.list_ub = reinterpret_cast<float*>(take((size_t)nqb * ncb * 4));
     P.counts = reinterpret_cast<uint32_t*>(take((size_t)nqb * 4));
@@ -428,16 +500,17 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist); note_launch();
     k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start); note_launch();
     k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm); note_launch();
-    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius); note_launch();
-    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius); note_launch();
+    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
+    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f);
+    note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t st) {
-    const size_t smem = 8192 * 8;
+    const size_t smem = (size_t)LIST_N * 8;
     cudaError_t e = cudaFuncSetAttribute(k_block_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_block_lists<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter, P.cradius, P.nqb, P.ncb, P.d, P.tq,
+    k_block_lists<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq,
                                               P.lists, P.list_ub, P.counts, P.ub_skip, skipped_total); note_launch();
     k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub); note_launch();
     return cudaGetLastError();

@@ -23,6 +23,8 @@ struct Plan {
     double* qradius;     // [nqb]
     double* ccenter;     // [ncb][d]
     double* cradius;     // [ncb]
+    float* ccenter_f;    // [d][ncb] the centres rounded to f32, transposed (for the f32 bound)
+    float* cradius_f;    // [ncb] the radii rounded up to f32
     uint32_t* lists;     // [nqb][ncb] kept column blocks, nearest first
     float* list_ub;      // [nqb][ncb] the bound of each list entry (non-increasing; +inf when unsorted)
     uint32_t* counts;    // [nqb]

@@ -105,47 +105,4 @@ __device__ __forceinline__ void warp_sort_keys(uint64_t (&v)[SL], int lane) {
     }
 }
 
-// Bitonic sort of a warp-distributed array (position p = s·32 + lane) into (score desc, index asc).
-template <int SL>
-__device__ __forceinline__ void warp_sort_f32(float (&sc)[SL], uint32_t (&id)[SL], int lane) {
-    constexpr int N = 32 * SL;
-#pragma unroll
-    for (int size = 2; size <= N; size <<= 1) {
-#pragma unroll
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (stride >= 32) {
-#pragma unroll
-                for (int s = 0; s < SL; ++s) {
-                    const int t = s ^ (stride >> 5);
-                    if (t > s) {
-                        const bool asc = ((s * 32 + lane) & size) == 0;
-                        const bool sw = asc ? better(sc[t], id[t], sc[s], id[s]) : better(sc[s], id[s], sc[t], id[t]);
-                        if (sw) {
-                            const float a = sc[s];
-                            sc[s] = sc[t];
-                            sc[t] = a;
-                            const uint32_t b = id[s];
-                            id[s] = id[t];
-                            id[t] = b;
-                        }
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int s = 0; s < SL; ++s) {
-                    const float os = __shfl_xor_sync(COSTAL_FULL_MASK, sc[s], stride);
-                    const uint32_t oi = __shfl_xor_sync(COSTAL_FULL_MASK, id[s], stride);
-                    const bool lower = (lane & stride) == 0;
-                    const bool asc = ((s * 32 + lane) & size) == 0;
-                    const bool take = (lower == asc) ? better(os, oi, sc[s], id[s]) : better(sc[s], id[s], os, oi);
-                    if (take) {
-                        sc[s] = os;
-                        id[s] = oi;
-                    }
-                }
-            }
-        }
-    }
-}
-
 }  // namespace costal

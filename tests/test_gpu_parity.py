@@ -102,7 +102,9 @@ def test_lcg_known_answers(ext, oracle):
 
 
 @pytest.mark.parametrize("n,d,k,margin", [(1001, 1, 5, None), (777, 5, 1, 0), (1500, 15, 10, 8), (1300, 17, 7, None),
-                                          (900, 33, 30, None), (640, 64, 12, 3), (2000, 40, 10, 118), (129, 3, 20, 0)])
+                                          (900, 33, 30, None), (640, 64, 12, 3), (2000, 40, 10, 118), (129, 3, 20, 0),
+                                          (700, 65, 10, None), (600, 300, 15, None), (500, 2000, 15, 15),
+                                          (300, 130, 40, 60)])
 def test_shapes_and_margins(ext, oracle, n, d, k, margin):
     rng = np.random.default_rng(n * 31 + d)
     means = rng.normal(0, 2, size=(7, d))
@@ -260,8 +262,9 @@ def test_mixture_20k_full_parity_and_labels(ext, oracle):
     np.testing.assert_array_equal(m, mo)
 
 
-@pytest.mark.parametrize("name,rows", [("rare_400k", 3000), ("dense_dup_160k", 2000), ("zipf_2m", 600)])
-@pytest.mark.parametrize("backend", ["fp32", "bf16"])
+@pytest.mark.parametrize("name,rows,backend", [(w, r, b) for w, r in (("rare_400k", 3000), ("dense_dup_160k", 2000),
+                                                                     ("zipf_2m", 600)) for b in ("fp32", "bf16")]
+                         + [("scrna_100k", 200, "fp32")])
 def test_full_size_row_sample_parity(ext, oracle, name, rows, backend):
     """Full-size inputs: the GPU answer for a seeded sample of query rows equals the oracle's
     answer for those rows against all n columns (bit-exact), and every row satisfies the output

@@ -95,6 +95,14 @@ def test_constant_threshold_ablation_and_checkpoint_round_trip(ext, zipf_case):
         got, st_c = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
         for a, b in zip(got, ref):
             np.testing.assert_array_equal(a, b)
+        # an over-confident threshold (the median k-th cosine): many skips are not certified, and those
+        # rows are rescanned over column segments whose lists are merged; the output stays exact
+        const[-1] = np.quantile(ref[1][:, wl.k - 1], 0.5)
+        ext._mlp_set(const, d, k, q)
+        got, st_h = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+        for a, b in zip(got, ref):
+            np.testing.assert_array_equal(a, b)
+        assert st_h["pruned_fallback_rows"] > 1000, st_h
     finally:
         ext._mlp_set(params, d, k, q)  # restore the trained model (checkpoint round trip)
     print("visited blocks: trained", _visited(st_mlp), "constant", _visited(st_c))
