@@ -17,6 +17,7 @@ inference and the block lists; the model itself is trained once before timing (r
   e2e    — the same through the host C-ABI call costal_build_graph: pinned host X in, pinned host
            edge list out, copies inside the timed region (wall clock around the synchronous call);
   plain_fp32 — the plain FP32 GPU path on the same input (device-resident, same timing);
+  without_learned — the certified BF16 path with the exact early stop but no learned threshold;
   roofline — the dominant kernel (the coarse tile + selection kernel): algorithmic FLOP/s (2·d per
            visited pair: pairs of the tiles neither skipped by the learned threshold nor left out by
            the exact early stop) over its CUDA-event duration;
@@ -191,6 +192,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="bf16 backend without the learned pruning")
     ap.add_argument("--train-sample", type=int, default=200_000)
     ap.add_argument("--train-epochs", type=int, default=30)
+    ap.add_argument("--train-quantile", type=float, default=0.05, help="pinball-loss quantile of the model")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP32 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -242,7 +244,7 @@ def main():
     if learned:
         mo = L.MlpOpts()
         mo.sample, mo.epochs, mo.batch = min(args.train_sample, n), args.train_epochs, 2048
-        mo.margin, mo.lr, mo.quantile, mo.seed = wl.margin, 2e-3, 0.05, 20241203
+        mo.margin, mo.lr, mo.quantile, mo.seed = wl.margin, 2e-3, args.train_quantile, 20241203
         ms_ = L.MlpStats()
         t = time.perf_counter()
         L.check(lib.costal_mlp_train(x.ctypes.data_as(C.c_void_p), n, d, k, C.byref(mo), C.byref(ms_), err, errlen),
@@ -342,6 +344,16 @@ def main():
                  "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in pstats])),
                  "speedup": pms / ms, "identical_edges": bool(same)}
 
+    # ---- the same certified path without the learned threshold (exact early stop only)
+    stop_only = None
+    if learned:
+        sms, sstats, _, sedges = timed_device(make_opts("bf16", False), 1, args.steps)
+        stop_only = {"ms_per_step": sms, "value": ws * n / (sms * 1e-3), "unit": "cells/s", "steps": args.steps,
+                     "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in sstats])),
+                     "blocks_stopped": sstats[-1]["blocks_stopped"], "same_edge_count": sedges == edges}
+        if plain is not None:
+            stop_only["speedup_vs_plain"] = plain["ms_per_step"] / sms
+
     if rank == 0:
         pk, pk_kind = peaks()
         s0 = stats[-1]
@@ -397,6 +409,7 @@ def main():
             "pair_dots_per_s": ws * float(n) * (n - 1) / (ms * 1e-3),
             "edges": edges,
             "plain_fp32": plain,
+            "without_learned": stop_only,
             "train": train,
             "stats": {kk: s0[kk] for kk in ("fallback_rows", "recomputed_rows", "pruned_fallback_rows",
                                              "blocks_skipped", "blocks_stopped", "blocks_total", "max_coarse_err", "ms_prep",

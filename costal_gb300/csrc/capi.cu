@@ -65,7 +65,7 @@ struct Context {
     DevBuf x, norms, xsT, cand_idx, cand_score, tau, out_idx, out_cos, out_w, fb_rows, fb_minsim, misc;
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
-    DevBuf part_idx, part_score, part_tau;
+    DevBuf part_idx, part_score, part_tau, tfloor;
     MlpState mlp;
 };
 
@@ -260,8 +260,12 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                     CK(ensure(c.part_score, (size_t)segs * nfail * cap * 4));
                     CK(ensure(c.part_tau, (size_t)segs * nfail * 4));
                 }
+                CK(ensure(c.tfloor, (size_t)n * 4));
+                CK(launch_rerun_floor(c.tc_rows.as<uint32_t>(), &dm->tc_fail_count, nfail, cap, c.tau.as<float>(),
+                                      c.cand_score.as<float>(), plan.row_eps, eps, c.tfloor.as<float>(), s));
                 CK(launch_coarse_fp32_split(c.xsT.as<float>(), n, np, dp, cap, cap, c.tc_rows.as<uint32_t>(),
-                                            &dm->tc_fail_count, nfail, segs, c.part_idx.as<uint32_t>(),
+                                            &dm->tc_fail_count, nfail, segs, c.tfloor.as<float>(),
+                                            c.part_idx.as<uint32_t>(),
                                             c.part_score.as<float>(), c.part_tau.as<float>(), c.cand_idx.as<uint32_t>(),
                                             c.cand_score.as<float>(), c.tau.as<float>(), s));
                 CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),

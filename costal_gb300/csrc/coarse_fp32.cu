@@ -76,12 +76,15 @@ __device__ __forceinline__ void write_lists(const float* L_s, const uint32_t* L_
 
 // The selection of one 128 × 128 tile, shared by both FP32 kernels: the admission test of the
 // thread's 8 × 8 scores against each query's τ at the tile start, the per-query buffer, and the
-// warp-local merges into the top-cap lists. `recompute(qi, cl)` returns the score of query slot qi
+// warp-local merges into the top-cap lists. τ is the worst kept score once cap are kept, before that
+// the query's floor (−inf, or a bound from an earlier pass below which no column can be among the
+// best cap). `recompute(qi, cl)` returns the score of query slot qi
 // and tile column cl with the same FMA order as the main loop (used when a buffer overflows).
 template <int SLOTS, class RowOf, class Recompute>
 __device__ __forceinline__ void select_tile(const float (&acc)[8][8], int c0, int n, int cap, float* L_s, uint32_t* L_i,
                                             float* buf_s, uint32_t* buf_i, int* cnt_s, int* len_s, float* tau_s,
-                                            int warp, int lane, int tx, int ty, RowOf row_of, Recompute recompute) {
+                                            const float* floor_s, int warp, int lane, int tx, int ty, RowOf row_of,
+                                            Recompute recompute) {
     constexpr int LCAP = 32 * SLOTS;
     auto qi_of = [&](int i) { return i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4); };
     auto cj_of = [&](int j) { return j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4); };
@@ -154,7 +157,7 @@ __device__ __forceinline__ void select_tile(const float (&acc)[8][8], int c0, in
             __syncwarp();
             if (lane == 0) {
                 len_s[qi] = len;
-                tau_s[qi] = len == cap ? worst : -CUDART_INF_F;
+                tau_s[qi] = len == cap ? worst : floor_s[qi];
                 cnt_s[qi] = 0;
             }
         }
@@ -166,7 +169,8 @@ template <int SLOTS, int DPC>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp_rt, int cap, int lstride,
                   const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
-                  uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
+                  const float* __restrict__ tfloor, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
+                  float* __restrict__ tau_out) {
     constexpr int LCAP = 32 * SLOTS;
     const int dp = DPC ? DPC : dp_rt;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -179,6 +183,7 @@ __global__ void __launch_bounds__(NT, 1)
     int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);       // [BM]
     int* len_s = cnt_s + BM;                                     // [BM]
     float* tau_s = reinterpret_cast<float*>(len_s + BM);         // [BM]
+    float* floor_s = tau_s + BM;                                 // [BM]
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = tid & 15, ty = tid >> 4;
@@ -212,13 +217,15 @@ __global__ void __launch_bounds__(NT, 1)
     for (int q = tid; q < BM; q += NT) {
         cnt_s[q] = 0;
         len_s[q] = 0;
-        tau_s[q] = -CUDART_INF_F;
+        const int r = row_of(q);
+        floor_s[q] = tfloor && r >= 0 ? tfloor[r] : -CUDART_INF_F;
+        tau_s[q] = floor_s[q];
     }
-    // Unfilled slots read back as column 0 with score −∞ (only possible with NaN input, which the
-    // host reports as an error): every index stays in range.
+    // Unfilled slots read back as index 0xffffffff with score −inf: an empty slot for the rescoring
+    // (a list can stay short only with NaN input or a floor at a tie).
     for (int e = tid; e < BM * LCAP; e += NT) {
         L_s[e] = -CUDART_INF_F;
-        L_i[e] = 0u;
+        L_i[e] = 0xffffffffu;
     }
 
     for (int tl = 0; tl < ntiles; ++tl) {
@@ -277,7 +284,8 @@ __global__ void __launch_bounds__(NT, 1)
         }
 #endif
 
-        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, warp, lane, tx, ty, row_of,
+        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
+                           row_of,
                            [&](int qi, int cl) {
                                float sv = 0.0f;
 #pragma unroll(DPC ? DPC : 4)
@@ -298,7 +306,8 @@ template <int SLOTS, int KC>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32_kc(const float* __restrict__ xsT, int n, int np, int dp, int cap, int lstride,
                      const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
-                     uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out) {
+                     const float* __restrict__ tfloor, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
+                     float* __restrict__ tau_out) {
     constexpr int LCAP = 32 * SLOTS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* S_s = reinterpret_cast<float*>(smem_raw);            // [STAGES][KC][BM + BN]
@@ -309,6 +318,7 @@ __global__ void __launch_bounds__(NT, 1)
     int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);       // [BM]
     int* len_s = cnt_s + BM;                                     // [BM]
     float* tau_s = reinterpret_cast<float*>(len_s + BM);         // [BM]
+    float* floor_s = tau_s + BM;                                 // [BM]
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tx = tid & 15, ty = tid >> 4;
@@ -352,11 +362,15 @@ __global__ void __launch_bounds__(NT, 1)
     for (int q = tid; q < BM; q += NT) {
         cnt_s[q] = 0;
         len_s[q] = 0;
-        tau_s[q] = -CUDART_INF_F;
+        const int r = row_of(q);
+        floor_s[q] = tfloor && r >= 0 ? tfloor[r] : -CUDART_INF_F;
+        tau_s[q] = floor_s[q];
     }
+    // Unfilled slots read back as index 0xffffffff with score −inf: an empty slot for the rescoring
+    // (a list can stay short only with NaN input or a floor at a tie).
     for (int e = tid; e < BM * LCAP; e += NT) {
         L_s[e] = -CUDART_INF_F;
-        L_i[e] = 0u;
+        L_i[e] = 0xffffffffu;
     }
 
     for (int tl = 0; tl < ntiles; ++tl) {
@@ -396,7 +410,8 @@ __global__ void __launch_bounds__(NT, 1)
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
-        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, warp, lane, tx, ty, row_of,
+        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
+                           row_of,
                            [&](int qi, int cl) {
                                // zero padding beyond dp adds exact zeros: the chain over dp is the same
                                const int q = row_of(qi);
@@ -416,19 +431,19 @@ constexpr int kc_for(int slots) { return slots <= 2 ? 32 : 16; }
 
 size_t coarse_smem_bytes_kc(int slots) {
     const size_t lcap = 32 * (size_t)slots;
-    return (size_t)STAGES * kc_for(slots) * (BM + BN) * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 + BM * 4 * 3;
+    return (size_t)STAGES * kc_for(slots) * (BM + BN) * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 + BM * 4 * 4;
 }
 
 template <int S>
 cudaError_t launch_kc(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                      const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
-                      float* tau, cudaStream_t st) {
+                      const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
+                      float* cand_score, float* tau, cudaStream_t st) {
     constexpr int KC = kc_for(S);
     const size_t smem = coarse_smem_bytes_kc(S);
     cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32_kc<S, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_coarse_fp32_kc<S, KC><<<dim3(np / BM, segs), NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount,
-                                                                   part_stride, cand_idx, cand_score, tau);
+    k_coarse_fp32_kc<S, KC><<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
+        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, cand_idx, cand_score, tau);
     note_launch();
     return cudaGetLastError();
 }
@@ -436,43 +451,44 @@ cudaError_t launch_kc(const float* xsT, int n, int np, int dp, int cap, int lstr
 size_t coarse_smem_bytes(int dp, int slots) {
     const size_t lcap = 32 * (size_t)slots;
     return (size_t)dp * BM * 4 + (size_t)STAGES * dp * BN * 4 + (size_t)BM * lcap * 8 + (size_t)BM * BUF * 8 +
-           BM * 4 * 3;
+           BM * 4 * 4;
 }
 
 template <int S, int D>
 cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
-                       float* tau, cudaStream_t st) {
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
+                       float* cand_score, float* tau, cudaStream_t st) {
     const size_t smem = coarse_smem_bytes(dp, S);
     cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_coarse_fp32<S, D><<<dim3(np / BM, segs), NT, smem, st>>>(xsT, n, np, dp, cap, lstride, qlist, qcount,
-                                                               part_stride, cand_idx, cand_score, tau);
+    k_coarse_fp32<S, D><<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
+        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, cand_idx, cand_score, tau);
     note_launch();
     return cudaGetLastError();
 }
 
 template <int S>
 cudaError_t dispatch_d(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
-                       float* tau, cudaStream_t st) {
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
+                       float* cand_score, float* tau, cudaStream_t st) {
 #define COSTAL_D(D)                                                                                            \
     case D:                                                                                                    \
-        return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx, \
-                                cand_score, tau, st);
+        return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, \
+                                cand_idx, cand_score, tau, st);
     switch (dp) {
         COSTAL_D(8) COSTAL_D(16) COSTAL_D(24) COSTAL_D(32) COSTAL_D(40) COSTAL_D(48) COSTAL_D(56) COSTAL_D(64)
         default:
-            return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx,
-                                    cand_score, tau, st);
+            return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride,
+                                    tfloor, cand_idx, cand_score, tau, st);
     }
 #undef COSTAL_D
 }
 
 cudaError_t launch_any(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int part_stride, uint32_t* cand_idx, float* cand_score,
-                       float* tau, cudaStream_t st) {
-#define COSTAL_ARGS xsT, n, np, dp, cap, lstride, qlist, qcount, segs, part_stride, cand_idx, cand_score, tau, st
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
+                       float* cand_score, float* tau, cudaStream_t st) {
+#define COSTAL_ARGS xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, cand_idx, cand_score, \
+    tau, st
     if (dp > 64) {  // deep rows: the chunked kernel
         switch (coarse_slots(cap)) {
             case 1: return launch_kc<1>(COSTAL_ARGS);
@@ -492,11 +508,12 @@ cudaError_t launch_any(const float* xsT, int n, int np, int dp, int cap, int lst
 
 // One warp per listed row: the union of its segments' lists (segs · cap ≤ 256 entries) sorted as
 // (score desc, index asc) keys; the best cap go to the row's candidates, and τ is the cap-th score
-// (≥ every segment's own τ, since a full segment list holds cap entries at or above it).
+// (≥ every segment's own τ, since a full segment list holds cap entries at or above it), or the
+// row's floor when the segments hold fewer than cap together.
 __global__ void k_merge_parts(const uint32_t* __restrict__ qlist, int count, int segs, int cap,
                               const uint32_t* __restrict__ part_idx, const float* __restrict__ part_score,
-                              int lstride, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
-                              float* __restrict__ tau_out) {
+                              const float* __restrict__ tfloor, int lstride, uint32_t* __restrict__ cand_idx,
+                              float* __restrict__ cand_score, float* __restrict__ tau_out) {
     const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (r >= count) return;
@@ -523,7 +540,8 @@ __global__ void k_merge_parts(const uint32_t* __restrict__ qlist, int count, int
         if (s == (cap - 1) >> 5) kth = key[s];
     }
     const uint64_t t = __shfl_sync(COSTAL_FULL_MASK, kth, (cap - 1) & 31);
-    if (lane == 0) tau_out[q] = key_score(t);
+    // with fewer than cap candidates in all segments together, the row's floor still bounds the rest
+    if (lane == 0) tau_out[q] = fmaxf(key_score(t), tfloor ? tfloor[q] : -CUDART_INF_F);
 }
 
 }  // namespace plain
@@ -537,7 +555,8 @@ int coarse_dpad(int d) { return d <= 64 ? ((d < 1 ? 1 : d) + 7) / 8 * 8 : (d + 3
 cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
                                const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
                                cudaStream_t st) {
-    return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, 0, cand_idx, cand_score, tau, st);
+    return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, 0, 0, nullptr, cand_idx, cand_score, tau,
+                             st);
 }
 
 int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
@@ -552,14 +571,38 @@ int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
 
 cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, int cap, int lstride,
                                      const uint32_t* qlist, const unsigned* qcount, int count, int segs,
-                                     uint32_t* part_idx, float* part_score, float* part_tau, uint32_t* cand_idx,
-                                     float* cand_score, float* tau, cudaStream_t st) {
-    if (segs <= 1) return launch_coarse_fp32(xsT, n, np, dp, cap, lstride, qlist, qcount, cand_idx, cand_score, tau, st);
-    cudaError_t e = plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, count, part_idx, part_score,
-                                      part_tau, st);
+                                     const float* tfloor, uint32_t* part_idx, float* part_score, float* part_tau,
+                                     uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
+    if (segs <= 1)
+        return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, count, 0, tfloor, cand_idx, cand_score,
+                                 tau, st);
+    cudaError_t e = plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, count, count, tfloor,
+                                      part_idx, part_score, part_tau, st);
     if (e != cudaSuccess) return e;
-    plain::k_merge_parts<<<(count + 7) / 8, 256, 0, st>>>(qlist, count, segs, cap, part_idx, part_score, lstride,
-                                                          cand_idx, cand_score, tau);
+    plain::k_merge_parts<<<(count + 7) / 8, 256, 0, st>>>(qlist, count, segs, cap, part_idx, part_score, tfloor,
+                                                          lstride, cand_idx, cand_score, tau);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// The re-run's floor for each listed row, from the tensor-core pass it follows: when that pass kept a
+// full list of cap candidates above its threshold τ, their exact cosines are ≥ τ − E_i, so the row's
+// cap-th FP32 score is ≥ τ − E_i − ε; below that no column can be among the best cap (rounded down).
+__global__ void k_rerun_floor(const uint32_t* __restrict__ rows, const unsigned* __restrict__ count, int cap,
+                              const float* __restrict__ tau, const float* __restrict__ cand_score,
+                              const double* __restrict__ row_eps, double eps, float* __restrict__ tfloor) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (int)*count) return;
+    const uint32_t i = rows[r];
+    const bool full = cand_score[(size_t)i * cap + cap - 1] > -CUDART_INF_F;
+    tfloor[i] = full ? __double2float_rd(__dsub_rd(__dsub_rd((double)tau[i], row_eps[i]), eps)) : -CUDART_INF_F;
+}
+
+cudaError_t launch_rerun_floor(const uint32_t* rows, const unsigned* count, int nmax, int cap, const float* tau,
+                               const float* cand_score, const double* row_eps, double eps, float* tfloor,
+                               cudaStream_t st) {
+    if (nmax <= 0) return cudaSuccess;
+    k_rerun_floor<<<(nmax + 255) / 256, 256, 0, st>>>(rows, count, cap, tau, cand_score, row_eps, eps, tfloor);
     note_launch();
     return cudaGetLastError();
 }

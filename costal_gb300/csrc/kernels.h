@@ -22,10 +22,15 @@ cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap,
 // Few listed rows: the columns split into `segs` segments (one CTA per 128 rows per segment), their
 // lists merged per row. part_* hold segs × count × cap entries (τ: segs × count).
 int coarse_fp32_segments(int count, int np, int cap, int sm_count);
+// tfloor (optional, by row): a per-row threshold below which no column can be among the best cap.
 cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, int cap, int lstride,
                                      const uint32_t* qlist, const unsigned* qcount, int count, int segs,
-                                     uint32_t* part_idx, float* part_score, float* part_tau, uint32_t* cand_idx,
-                                     float* cand_score, float* tau, cudaStream_t st);
+                                     const float* tfloor, uint32_t* part_idx, float* part_score, float* part_tau,
+                                     uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st);
+// The floor of rows re-run after the tensor-core pass (rows[0..*count), cand_* and tau of that pass).
+cudaError_t launch_rerun_floor(const uint32_t* rows, const unsigned* count, int nmax, int cap, const float* tau,
+                               const float* cand_score, const double* row_eps, double eps, float* tfloor,
+                               cudaStream_t st);
 cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
                            const float* cand_score, const float* tau, const double* norms, const double* row_eps,
                            const double* row_ub, unsigned* ub_fail, double eps, int certify, int select,

@@ -298,14 +298,15 @@ __device__ __forceinline__ void group_max8(const uint32_t (&r)[64], float* gm) {
     for (int g = 0; g < 8; ++g) gm[g] = max8(r + 8 * g);
 }
 
-// The cap-th largest of 32 values (cap ≤ 32): a bitonic sorting network in registers.
-__device__ __forceinline__ float kth_of_32(float (&v)[32], int cap) {
+// The cap-th largest of N values (cap ≤ N, N a power of two): a bitonic sorting network in registers.
+template <int N>
+__device__ __forceinline__ float kth_of(float (&v)[N], int cap) {
 #pragma unroll
-    for (int size = 2; size <= 32; size <<= 1) {
+    for (int size = 2; size <= N; size <<= 1) {
 #pragma unroll
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
+            for (int i = 0; i < N; ++i) {
                 const int j = i ^ stride;
                 if (j > i) {
                     const float a = v[i], b = v[j];
@@ -318,9 +319,17 @@ __device__ __forceinline__ float kth_of_32(float (&v)[32], int cap) {
     }
     float t = v[0];
 #pragma unroll
-    for (int i = 0; i < 32; ++i)
+    for (int i = 0; i < N; ++i)
         if (i == cap - 1) t = v[i];
     return t;
+}
+
+// The 16 four-column group maxima of a 64-column slice.
+__device__ __forceinline__ void group_max4(const uint32_t (&r)[64], float* gm) {
+#pragma unroll
+    for (int g = 0; g < 16; ++g)
+        gm[g] = fmaxf(max3f(__uint_as_float(r[4 * g]), __uint_as_float(r[4 * g + 1]), __uint_as_float(r[4 * g + 2])),
+                      __uint_as_float(r[4 * g + 3]));
 }
 
 // One 64-column slice held in registers: a per-lane 8-bit mask of the 8-column groups whose maximum
@@ -505,19 +514,33 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (*reinterpret_cast<volatile int*>(&bars->stop_tile) == t) break;
             const int c0 = block_of(t) * BLOCK_N;
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
-            if (t == 0 && cap <= 32) {
-                // A starting threshold from the first tile: the cap-th largest of its 32 column-group
-                // maxima is reached by cap distinct columns, so it is a valid lower bound of the
-                // query's cap-th score. The first tile itself is admitted at ≥ τ₀ (one below in the
-                // strict test), later tiles at > τ as usual.
-                float gmax[32];
+            if (t == 0) {
+                // A starting threshold from the first tile: the cap-th largest of its column-group
+                // maxima (32 groups of 8 columns, or 64 of 4 when cap > 32) is reached by cap distinct
+                // columns, so no other column below it can be among the query's best cap. (When the
+                // query's own column or padding supplies one of those maxima, τ₀ can be a little too
+                // high; that only costs the certificate, since τ never falls and everything left out
+                // stays below it.) The first tile itself is admitted at ≥ τ₀ (one below in the strict
+                // test), later tiles at > τ as usual.
+                if (cap <= 32) {
+                    float gmax[32];
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    tmem_ld64(tb + (uint32_t)(64 * h), ra);
-                    tmem_wait(ra);
-                    group_max8(ra, gmax + 8 * h);
+                    for (int h = 0; h < 4; ++h) {
+                        tmem_ld64(tb + (uint32_t)(64 * h), ra);
+                        tmem_wait(ra);
+                        group_max8(ra, gmax + 8 * h);
+                    }
+                    tau = nextafterf(kth_of<32>(gmax, cap), -CUDART_INF_F);
+                } else {
+                    float gmax[64];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        tmem_ld64(tb + (uint32_t)(64 * h), ra);
+                        tmem_wait(ra);
+                        group_max4(ra, gmax + 16 * h);
+                    }
+                    tau = nextafterf(kth_of<64>(gmax, cap), -CUDART_INF_F);
                 }
-                tau = nextafterf(kth_of_32(gmax, cap), -CUDART_INF_F);
             }
             // Four 64-column slices, as a two-step software pipeline: the next slice's TMEM load is
             // in flight while one is scanned. A slice costs a max tree and a warp OR; only the
@@ -687,7 +710,7 @@ static size_t fixed_smem(int nkb, int cap) {
 bool supported(int d, int cap) {
     if (d < 1 || 3 * d > 128 || cap < 1 || cap > 64) return false;
     const int nkb = kpad(d) / KB;
-    return fixed_smem(nkb, cap) + 2ull * nkb * B_KB_BYTES <= 227 * 1024;
+    return fixed_smem(nkb, cap) + (size_t)nkb * B_KB_BYTES <= 227 * 1024;  // at least one stage
 }
 
 size_t workspace_bytes(int n, int d) {
@@ -784,7 +807,7 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     const int ksteps = (3 * plan.d + 15) / 16;
     const size_t fixed = fixed_smem(nkb, cap);
     int stages = 4;
-    while (stages > 2 && fixed + (size_t)stages * nkb * B_KB_BYTES > 227 * 1024) --stages;
+    while (stages > 1 && fixed + (size_t)stages * nkb * B_KB_BYTES > 227 * 1024) --stages;
     const size_t smem = fixed + (size_t)stages * nkb * B_KB_BYTES;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;

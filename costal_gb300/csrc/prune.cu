@@ -242,12 +242,15 @@ constexpr double XI = 1e-6;
 // so acos(dot + δ) with δ = (d + 4)·2⁻²³, the sum rounded up, never exceeds the centres' angle;
 // acosf and cosf are within a few ulp, covered by 1e-6 on each side; every subtraction rounds down
 // and the final addition up. Radii arrive rounded up to f32.
-__device__ __forceinline__ float block_ub_f32(const float* cq, float rq, const float* cb, int cstride, float rb, int d) {
+// Also returns (in *phi_out) the centres' angle, used only to order blocks of equal bound.
+__device__ __forceinline__ float block_ub_f32(const float* cq, float rq, const float* cb, int cstride, float rb, int d,
+                                             float* phi_out = nullptr) {
     float dot = 0.0f;
     for (int t = 0; t < d; ++t) dot = fmaf(cq[t], cb[(size_t)t * cstride], dot);
     const float delta = (float)(d + 4) * 0x1p-23f;
     const float c = fminf(1.0f, __fadd_ru(dot, delta));
     const float phi = __fsub_rd(acosf(c), 1e-6f);
+    if (phi_out) *phi_out = phi;
     const float th = __fsub_rd(__fsub_rd(__fsub_rd(phi, rq), rb), (float)XI);
     if (th <= 0.0f) return 1.0f;
     return fminf(1.0f, __fadd_ru(cosf(th), 1e-6f));
@@ -270,7 +273,7 @@ __device__ __forceinline__ void cx_regs(uint64_t (&v)[LIST_KPT], int base, int s
 }
 
 // One CTA per query block: the upper bound against every column block; the blocks kept (UB ≥ t_Q)
-// sorted by (UB desc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
+// sorted by (UB desc, centre angle asc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
 // exchanged in registers, by warp shuffles or through shared memory by distance — and the largest UB
 // of a skipped block. Lists longer than LIST_N stay in block order with bounds +inf.
 __global__ void __launch_bounds__(LIST_T)
@@ -321,13 +324,18 @@ __global__ void __launch_bounds__(LIST_T)
             const int b = j * LIST_T + tid;
             v[j] = 0ull;  // absent or skipped: sorts last
             if (b < ncb) {
-                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d);
+                float phi;
+                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d, &phi);
                 if (u >= t) {
                     ++my_kept;
                     // the bound (possibly negative) as an order-preserving u32 above the complemented id
                     const uint32_t ub = __float_as_uint(u);
                     const uint32_t hk = (ub & 0x80000000u) ? ~ub : (ub | 0x80000000u);
-                    v[j] = ((uint64_t)hk << 32) | (uint64_t)(~(uint32_t)b);
+                    // ties of the bound (e.g. every block of the query's own cluster at 1) go nearest
+                    // centre first, then by block: the low word is (2^19 − 1 − φ quantised) · 2^13 + (8191 − b)
+                    const uint32_t qphi = (uint32_t)fminf(524287.0f, fmaxf(0.0f, phi) * (524288.0f / 3.14159265f));
+                    const uint32_t lo = ((524287u - qphi) << 13) | (8191u - (uint32_t)b);
+                    v[j] = ((uint64_t)hk << 32) | (uint64_t)lo;
                 } else {
                     // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
                     my_skip = max(my_skip, __float_as_int(fmaxf(u, 0.0f)));
@@ -380,7 +388,7 @@ __global__ void __launch_bounds__(LIST_T)
             const unsigned e = (unsigned)(base + j);
             if (e < nk) {
                 const uint32_t hk = (uint32_t)(v[j] >> 32);
-                out[e] = ~(uint32_t)v[j];
+                out[e] = 8191u - ((uint32_t)v[j] & 8191u);
                 out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
             }
         }
