@@ -167,6 +167,13 @@ __device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOT
     }
 }
 
+// Two phases per CTA of 8 rows. (1) Every thread rescores candidates of the flattened (row, slot)
+// list — all lanes busy whatever cap is, since the f64 dot products are the kernel's cost on the
+// GB300's narrow FP64 pipe — into shared memory. (2) One warp per row sorts its cap results,
+// certifies and writes the row.
+constexpr int RS_ROWS = 8;
+constexpr int RS_MAXCAP = 128;
+
 template <int SLOTS>
 __global__ void __launch_bounds__(256)
     k_rescore(const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
@@ -177,22 +184,25 @@ __global__ void __launch_bounds__(256)
               const unsigned* __restrict__ rcount, uint32_t* __restrict__ out_idx, double* __restrict__ out_cos,
               double* __restrict__ out_w, uint32_t* __restrict__ fb_rows, double* __restrict__ fb_minsim,
               unsigned* __restrict__ fb_count, unsigned long long* __restrict__ max_err_bits) {
-    const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (w >= (rlist ? (int)*rcount : n)) return;
-    const int i = rlist ? (int)rlist[w] : w;
-    const double ni = norms[i];
-    const float* xi = x + (size_t)i * d;
+    __shared__ double sc_s[RS_ROWS * RS_MAXCAP], cs_s[RS_ROWS * RS_MAXCAP];
+    __shared__ uint32_t id_s[RS_ROWS * RS_MAXCAP];
+    __shared__ int row_s[RS_ROWS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nrows = rlist ? (int)*rcount : n;
+    const int w0 = blockIdx.x * RS_ROWS;
+    if (w0 >= nrows) return;
+    const int nr = min(RS_ROWS, nrows - w0);
+    if (tid < RS_ROWS) row_s[tid] = tid < nr ? (rlist ? (int)rlist[w0 + tid] : w0 + tid) : 0;
+    __syncthreads();
     const bool vec4 = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
-    double sc[SLOTS], cs[SLOTS];
-    uint32_t id[SLOTS];
     double err = 0.0;
-#pragma unroll
-    for (int s = 0; s < SLOTS; ++s) {
-        const int p = s * 32 + lane;
-        const uint32_t j = p < cap ? cand_idx[(size_t)i * lstride + p] : 0xffffffffu;
+    for (int e = tid; e < nr * cap; e += blockDim.x) {
+        const int r = e / cap, p = e - r * cap;
+        const int i = row_s[r];
+        const uint32_t j = cand_idx[(size_t)i * lstride + p];
         if (j < (uint32_t)n) {
             // (an index ≥ n marks an empty slot: the coarse pass kept fewer than cap candidates)
+            const float* xi = x + (size_t)i * d;
             const float* xj = x + (size_t)j * d;
             double dot = 0.0;
             if (vec4) {  // the same dimension order, 16-byte loads
@@ -207,25 +217,39 @@ __global__ void __launch_bounds__(256)
             } else {
                 for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
             }
-            const double nj = norms[j];
+            const double ni = norms[i], nj = norms[j];
             const double c = cos64(dot, ni, nj);
             const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
             err = fmax(err, fabs((double)cand_score[(size_t)i * lstride + p] - score));
-            sc[s] = score;
-            cs[s] = c;
-            id[s] = j;
+            sc_s[e] = score;
+            cs_s[e] = c;
+            id_s[e] = j;
         } else {
-            sc[s] = -CUDART_INF;
-            cs[s] = 0.0;
-            id[s] = 0xffffffffu;
+            sc_s[e] = -CUDART_INF;
+            cs_s[e] = 0.0;
+            id_s[e] = 0xffffffffu;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
     // one address for the whole grid: read it first, so that only a new maximum pays for the atomic
-    if (lane == 0 && max_err_bits) {
+    if (lane == 0 && max_err_bits && err > 0.0) {
         const unsigned long long eb = (unsigned long long)__double_as_longlong(err);
         if (eb > *reinterpret_cast<volatile unsigned long long*>(max_err_bits)) atomicMax(max_err_bits, eb);
+    }
+    __syncthreads();
+    if (warp >= nr) return;  // no barrier below
+    const int i = row_s[warp];
+    const double ni = norms[i];
+    double sc[SLOTS], cs[SLOTS];
+    uint32_t id[SLOTS];
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+        const int p = s * 32 + lane;
+        const bool v = p < cap;
+        sc[s] = v ? sc_s[warp * cap + p] : -CUDART_INF;
+        cs[s] = v ? cs_s[warp * cap + p] : 0.0;
+        id[s] = v ? id_s[warp * cap + p] : 0xffffffffu;
     }
     warp_sort<SLOTS>(sc, cs, id, lane);
     const double s_k = __shfl_sync(COSTAL_FULL_MASK, sc[(k - 1) >> 5], (k - 1) & 31);

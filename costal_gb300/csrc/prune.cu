@@ -276,7 +276,7 @@ __device__ __forceinline__ void cx_regs(uint64_t (&v)[LIST_KPT], int base, int s
 // sorted by (UB desc, centre angle asc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
 // exchanged in registers, by warp shuffles or through shared memory by distance — and the largest UB
 // of a skipped block. Lists longer than LIST_N stay in block order with bounds +inf.
-__global__ void __launch_bounds__(LIST_T)
+__global__ void __launch_bounds__(LIST_T, 2)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
                   const float* __restrict__ ccenter_f, const float* __restrict__ cradius_f, int nqb, int ncb, int d,
                   const float* __restrict__ tq, uint32_t* __restrict__ lists, float* __restrict__ list_ub,
