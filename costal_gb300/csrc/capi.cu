@@ -213,27 +213,33 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         CK(ensure(c.cand_score, (size_t)n * cap * 4));
         CK(ensure(c.tau, (size_t)n * 4));
         const double eps = ((double)d + 4.0) * F32_EPS;  // knn.rs:185-187
-        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap) && prune::supported(d)) {
+        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap)) {
             used_tc = true;
             // Locality order (k-means cells) and per-query-block column lists, nearest blocks first;
-            // with a learned threshold, blocks whose bound is below it are skipped.
-            CK(ensure(c.prune_ws, prune::workspace_bytes(n, d)));
+            // with a learned threshold, blocks whose bound is below it are skipped. Deep rows (the
+            // pruning geometry covers d ≤ 64) keep the input order and visit every column block.
+            const bool ordered = prune::supported(d);
             prune::Plan pp{};
-            CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), n, np, d, s, pp));
-            const bool learned = o.learned_prune && c.mlp.ready && c.mlp.d == d && c.mlp.k == k;
-            if (learned) {
-                CK(mlp_predict_thresholds(c, pp, s));
-            } else {
-                pp.tq = nullptr;
+            bool learned = false;
+            if (ordered) {
+                CK(ensure(c.prune_ws, prune::workspace_bytes(n, d)));
+                CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), n, np, d, s, pp));
+                learned = o.learned_prune && c.mlp.ready && c.mlp.d == d && c.mlp.k == k;
+                if (learned) {
+                    CK(mlp_predict_thresholds(c, pp, s));
+                } else {
+                    pp.tq = nullptr;
+                }
+                CK(prune::build_lists(pp, &dm->blocks_skipped, s));
             }
-            CK(prune::build_lists(pp, &dm->blocks_skipped, s));
             CK(cudaEventRecord(c.ev[5], s));
             CK(ensure(c.tc_ws, tc::workspace_bytes(n, d)));
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
-            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, pp.perm, s, plan));
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan));
             CK(cudaEventRecord(c.ev[6], s));
-            CK(tc::launch_coarse(plan, cap, pp.lists, o.prune ? pp.list_ub : nullptr, pp.counts, pp.ncb, c.cand_idx.as<uint32_t>(),
+            CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr, ordered && o.prune ? pp.list_ub : nullptr,
+                                 ordered ? pp.counts : nullptr, ordered ? pp.ncb : 0, c.cand_idx.as<uint32_t>(),
                                  c.cand_score.as<float>(), c.tau.as<float>(), &dm->blocks_stopped, &dm->timeout_flag,
                                  c.sm_count, s));
             CK(cudaEventRecord(c.ev[2], s));

@@ -373,7 +373,7 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
     *tau_io = tau;
 }
 
-template <int SLOTS>
+template <int SLOTS, bool KLOOP>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
                 int nkb, int ksteps, int stages, int cap, const uint32_t* __restrict__ perm,
@@ -387,9 +387,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // 1024-byte alignment for the swizzled tiles
     const uint32_t base_u32 = smem_u32(smem_raw);
     unsigned char* smem = smem_raw + ((1024 - (base_u32 & 1023)) & 1023);
-    unsigned char* a_tile = smem;                                   // nkb × 16 KB
-    unsigned char* b_tiles = a_tile + (size_t)nkb * A_KB_BYTES;     // stages × nkb × 32 KB
-    float* B_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * nkb * B_KB_BYTES);  // [BCAP][BSTRIDE]
+    // Resident A: the query tile (nkb K blocks) once, then `stages` column tiles of nkb K blocks.
+    // K loop (deep rows, KLOOP): every stage holds one K block of the query tile and of the column
+    // tile, and a tile's MMA chain runs over nkb stages.
+    const uint32_t stage_bytes = KLOOP ? (uint32_t)(A_KB_BYTES + B_KB_BYTES) : (uint32_t)nkb * B_KB_BYTES;
+    unsigned char* a_tile = smem;                                            // nkb × 16 KB (resident A)
+    unsigned char* b_tiles = KLOOP ? smem : a_tile + (size_t)nkb * A_KB_BYTES;  // stages × stage_bytes
+    float* B_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * stage_bytes);  // [BCAP][BSTRIDE]
     uint32_t* B_i = reinterpret_cast<uint32_t*>(B_s + BCAP * BSTRIDE);
     Barriers* bars = reinterpret_cast<Barriers*>(B_i + BCAP * BSTRIDE);
 
@@ -401,6 +405,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t* my_list = lists ? lists + (size_t)blockIdx.x * ncb : nullptr;
     auto block_of = [&](int t) -> int { return my_list ? (int)my_list[t] : t; };
     const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb * B_KB_BYTES;
+    (void)a_bytes;
 
     if (threadIdx.x == 0) {
         mbar_init(&bars->a_full, 1);
@@ -429,7 +434,46 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
     if (warp == EPI_WARPS) {
         // ------------------------------------------------------------------ TMA producer
-        if (lane == 0) {
+        if (KLOOP && lane == 0) {
+            const float* my_ub = list_ub ? list_ub + (size_t)blockIdx.x * ncb : nullptr;
+            bool go = true;
+            for (int t = 0; go && t < ntiles; ++t) {
+                const int cb = block_of(t) * BLOCK_N;
+                for (int kb = 0; kb < nkb; ++kb) {
+                    const int g = t * nkb + kb, s = g % stages;
+                    const uint32_t ph = (uint32_t)(g / stages) & 1u;
+                    if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) {
+                        go = false;
+                        break;
+                    }
+                    if (kb == 0) {
+                        bool stop = false;
+                        if ((unsigned)block_of(t) >= (unsigned)(np / BLOCK_N)) {
+                            atomicExch(timeout_flag, 2ull);  // never produced by the list kernel
+                            stop = true;
+                        } else if (t > 0 && my_ub) {
+                            volatile float* wf = bars->warp_floor;
+                            const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
+                            if (my_ub[t] < fl) {
+                                stop = true;
+                                if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
+                            }
+                        }
+                        if (stop) {
+                            *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
+                            mbar_arrive(&bars->b_full[s]);
+                            go = false;
+                            break;
+                        }
+                    }
+                    mbar_expect_tx(&bars->b_full[s], (uint32_t)(A_KB_BYTES + B_KB_BYTES));
+                    unsigned char* dst = b_tiles + (size_t)s * stage_bytes;
+                    tma_load_2d(dst, &map_a, kb * KB, q0, &bars->b_full[s]);
+                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
+                }
+            }
+        }
+        if (!KLOOP && lane == 0) {
             mbar_expect_tx(&bars->a_full, a_bytes);
             for (int kb = 0; kb < nkb; ++kb) tma_load_2d(a_tile + kb * A_KB_BYTES, &map_a, kb * KB, q0, &bars->a_full);
             const float* my_ub = list_ub ? list_ub + (size_t)blockIdx.x * ncb : nullptr;
@@ -467,7 +511,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
     } else if (warp == EPI_WARPS + 1) {
         // ------------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
+        if (KLOOP && lane == 0) {
+            bool go = true;
+            for (int t = 0; go && t < ntiles; ++t) {
+                const int buf = t & 1;
+                const uint32_t bph = (uint32_t)(t >> 1) & 1u;
+                if (!mbar_wait(&bars->t_empty[buf], bph ^ 1u, timeout_flag, true)) break;
+                const uint32_t d = tmem + (uint32_t)(buf * BLOCK_N);
+                for (int kb = 0; kb < nkb; ++kb) {
+                    const int g = t * nkb + kb, s = g % stages;
+                    const uint32_t ph = (uint32_t)(g / stages) & 1u;
+                    if (!mbar_wait(&bars->b_full[s], ph, timeout_flag, true)) {
+                        go = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    if (kb == 0 && *reinterpret_cast<volatile int*>(&bars->stop_tile) == t) {
+                        mbar_arrive(&bars->t_full[buf]);  // pass the stop on to the epilogue warps
+                        go = false;
+                        break;
+                    }
+                    const uint32_t a_base = smem_u32(b_tiles + (size_t)s * stage_bytes);
+                    const uint32_t b_base = a_base + A_KB_BYTES;
+                    const int nks = min(4, ksteps - 4 * kb);
+                    for (int ks = 0; ks < nks; ++ks) {
+                        const uint32_t koff = (uint32_t)(ks * 32);  // 16 bf16 = 32 bytes inside the swizzle row
+                        mma_bf16(d, sw128_desc(a_base + koff), sw128_desc(b_base + koff), (kb | ks) ? 1u : 0u);
+                    }
+                    mma_commit(&bars->b_empty[s]);
+                }
+                if (!go) break;
+                mma_commit(&bars->t_full[buf]);
+            }
+        }
+        if (!KLOOP && lane == 0) {
             bool ok = mbar_wait(&bars->a_full, 0, timeout_flag, true);
             tc_fence_after();
             const uint32_t a_base = smem_u32(a_tile);
@@ -682,6 +759,62 @@ __global__ void __launch_bounds__(SPLIT_ROWS)
     }
 }
 
+// The same split for deep rows (operands too wide for k_split's shared-memory staging): one CTA
+// per working row, 256 threads over its dimensions, the four f64 piece norms by a fixed-order tree.
+__global__ void __launch_bounds__(256)
+    k_split_wide(const float* __restrict__ xsT, int n, int np_x, int d, int kp, const uint32_t* __restrict__ perm,
+                 __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
+                 unsigned long long* __restrict__ colmax) {
+    __shared__ double red[4][256];
+    const int r = blockIdx.x, tid = threadIdx.x;
+    const bool live = r < n;
+    const int o = live ? (perm ? (int)perm[r] : r) : 0;
+    __nv_bfloat16* ra = opa + (size_t)r * kp;
+    __nv_bfloat16* rb = opb + (size_t)r * kp;
+    double sh = 0.0, sl = 0.0, sr = 0.0, sp = 0.0;
+    for (int t = tid; t < d; t += 256) {
+        const float a = live ? xsT[(size_t)t * np_x + o] : 0.0f;
+        const __nv_bfloat16 hb = __float2bfloat16_rn(a);
+        const float h = __bfloat162float(hb);
+        const float e = a - h;  // exact in f32
+        const __nv_bfloat16 lb = __float2bfloat16_rn(e);
+        const float l = __bfloat162float(lb);
+        const float rem = e - l;  // exact in f32
+        ra[t] = hb;
+        ra[d + t] = lb;
+        ra[2 * d + t] = hb;
+        rb[t] = hb;
+        rb[d + t] = hb;
+        rb[2 * d + t] = lb;
+        sh = __fma_rn((double)h, (double)h, sh);
+        sl = __fma_rn((double)l, (double)l, sl);
+        sr = __fma_rn((double)rem, (double)rem, sr);
+        const double p = (double)h + (double)l;
+        sp = __fma_rn(p, p, sp);
+    }
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
+    for (int t = 3 * d + tid; t < kp; t += 256) {
+        ra[t] = zero;
+        rb[t] = zero;
+    }
+    red[0][tid] = sh;
+    red[1][tid] = sl;
+    red[2][tid] = sr;
+    red[3][tid] = sp;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (tid < h)
+            for (int j = 0; j < 4; ++j) red[j][tid] += red[j][tid + h];
+        __syncthreads();
+    }
+    if (tid < 4 && live) {
+        const double v = sqrt(red[tid][0]);
+        pnorm[(size_t)tid * n + o] = v;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        if (b > *reinterpret_cast<volatile unsigned long long*>(&colmax[tid])) atomicMax(&colmax[tid], b);
+    }
+}
+
 __global__ void k_row_eps(const double* __restrict__ pnorm, const unsigned long long* __restrict__ colmax, int n,
                           int d, int keff, double* __restrict__ row_eps) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -702,15 +835,21 @@ __global__ void k_row_eps(const double* __restrict__ pnorm, const unsigned long 
 
 static int kpad(int d) { return (3 * d + KB - 1) / KB * KB; }
 
+// Up to two K blocks (3d ≤ 128) the query tile stays resident; deeper rows run the K loop.
+static bool kloop(int nkb) { return nkb > 2; }
+
 static size_t fixed_smem(int nkb, int cap) {
     const int bcap = cap <= 32 ? 64 : 128;
-    return 1024 + (size_t)nkb * A_KB_BYTES + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
+    return 1024 + (kloop(nkb) ? 0 : (size_t)nkb * A_KB_BYTES) + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
+}
+static size_t stage_smem(int nkb) {
+    return kloop(nkb) ? (size_t)(A_KB_BYTES + B_KB_BYTES) : (size_t)nkb * B_KB_BYTES;
 }
 
 bool supported(int d, int cap) {
-    if (d < 1 || 3 * d > 128 || cap < 1 || cap > 64) return false;
+    if (d < 1 || cap < 1 || cap > 64) return false;
     const int nkb = kpad(d) / KB;
-    return fixed_smem(nkb, cap) + (size_t)nkb * B_KB_BYTES <= 227 * 1024;  // at least one stage
+    return fixed_smem(nkb, cap) + stage_smem(nkb) <= 227 * 1024;  // at least one stage
 }
 
 size_t workspace_bytes(int n, int d) {
@@ -777,10 +916,14 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     if (e != cudaSuccess) return e;
     // xsT has ⌈n/128⌉·128 columns; operand rows in [n, np) are zero-filled by k_split itself.
     const size_t smem = (size_t)2 * SPLIT_ROWS * (kp / 2 + 1) * 4;
-    e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, kp, perm, L.opa, L.opb, L.pnorm,
-                                                        L.colmax);
+    if (smem <= 227 * 1024) {
+        e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, kp, perm, L.opa, L.opb, L.pnorm,
+                                                            L.colmax);
+    } else {
+        k_split_wide<<<np, 256, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax);
+    }
     note_launch();
     k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps); note_launch();
     plan.n = n;
@@ -805,13 +948,14 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
         return cudaErrorInvalidValue;
     const int nkb = plan.kp / KB;
     const int ksteps = (3 * plan.d + 15) / 16;
-    const size_t fixed = fixed_smem(nkb, cap);
+    const size_t fixed = fixed_smem(nkb, cap), per = stage_smem(nkb);
     int stages = 4;
-    while (stages > 1 && fixed + (size_t)stages * nkb * B_KB_BYTES > 227 * 1024) --stages;
-    const size_t smem = fixed + (size_t)stages * nkb * B_KB_BYTES;
+    while (stages > 1 && fixed + (size_t)stages * per > 227 * 1024) --stages;
+    const size_t smem = fixed + (size_t)stages * per;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
-    auto kern = cap <= 32 ? k_coarse_tc<1> : k_coarse_tc<2>;
+    auto kern = kloop(nkb) ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
+                           : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, plan.perm, lists,

@@ -115,6 +115,17 @@ def test_shapes_and_margins(ext, oracle, n, d, k, margin):
     same(as_oracle(got), oracle.knn_bruteforce(x, k))
 
 
+@pytest.mark.parametrize("n,d,k,margin", [(700, 43, 10, None), (600, 300, 15, None), (500, 2000, 15, 15),
+                                          (400, 130, 20, 40)])
+def test_deep_rows_on_the_tensor_cores(ext, oracle, n, d, k, margin):
+    """Rows deeper than two K blocks run the tensor-core K loop (no locality order): same exact output."""
+    rng = np.random.default_rng(n + d)
+    means = rng.normal(0, 2, size=(9, d))
+    x = np.arcsinh((means[rng.integers(0, 9, n)] + rng.normal(0, 0.6, size=(n, d))) / 5.0).astype(np.float32)
+    got, st = ext._knn_exact(x, k, margin=margin, matmul="bf16")
+    same(as_oracle(got), oracle.knn_bruteforce(x, k))
+
+
 def test_tanimoto_selection_matches_bruteforce(ext, oracle):
     # test_knn.py:118-126
     x = clustered(1500, 12, 14)
@@ -264,7 +275,7 @@ def test_mixture_20k_full_parity_and_labels(ext, oracle):
 
 @pytest.mark.parametrize("name,rows,backend", [(w, r, b) for w, r in (("rare_400k", 3000), ("dense_dup_160k", 2000),
                                                                      ("zipf_2m", 600)) for b in ("fp32", "bf16")]
-                         + [("scrna_100k", 200, "fp32")])
+                         + [("scrna_100k", 200, "fp32"), ("scrna_100k", 200, "bf16")])
 def test_full_size_row_sample_parity(ext, oracle, name, rows, backend):
     """Full-size inputs: the GPU answer for a seeded sample of query rows equals the oracle's
     answer for those rows against all n columns (bit-exact), and every row satisfies the output
