@@ -592,14 +592,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int c0 = block_of(t) * BLOCK_N;
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
             if (t == 0) {
-                // A starting threshold from the first tile: the cap-th largest of its column-group
-                // maxima (32 groups of 8 columns, or 64 of 4 when cap > 32) is reached by cap distinct
-                // columns, so no other column below it can be among the query's best cap. (When the
+                // A starting threshold from the first tiles: the cap-th largest of their column-group
+                // maxima (64 groups of 8 columns over tiles 0 and 1, 32 over tile 0 alone, or 64 of 4
+                // when cap > 32) is reached by cap distinct columns, so no other column below it can
+                // be among the query's best cap. (When the
                 // query's own column or padding supplies one of those maxima, τ₀ can be a little too
                 // high; that only costs the certificate, since τ never falls and everything left out
                 // stays below it.) The first tile itself is admitted at ≥ τ₀ (one below in the strict
                 // test), later tiles at > τ as usual.
-                if (cap <= 32) {
+                if (cap <= 32 && ntiles >= 2) {
+                    // both accumulators hold a tile by now (tiles 0 and 1): 64 groups of 512 columns
+                    if (!mbar_wait(&bars->t_full[1], 0, timeout_flag, false)) break;
+                    tc_fence_after();
+                    // (no stop can fall on tile 1: the warps' floors are still −inf when it is issued)
+                    float gmax[64];
+#pragma unroll
+                    for (int h = 0; h < 8; ++h) {
+                        tmem_ld64(lane_addr + (uint32_t)((h >> 2) * BLOCK_N + 64 * (h & 3)), ra);
+                        tmem_wait(ra);
+                        group_max8(ra, gmax + 8 * h);
+                    }
+                    tau = nextafterf(kth_of<64>(gmax, cap), -CUDART_INF_F);
+                } else if (cap <= 32) {
                     float gmax[32];
 #pragma unroll
                     for (int h = 0; h < 4; ++h) {
