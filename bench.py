@@ -111,17 +111,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def traffic_per_launch(backend, pairs):
-    """DRAM bytes (read + write) per launch of the dominant kernel: bytes per visited pair from the
-    committed ncu capture summary profiles/dram_traffic.json, times this launch's visited pairs.
-    None when no capture exists for the backend."""
+def traffic_per_launch(backend, pairs, d):
+    """DRAM bytes (read + write) per launch of the dominant kernel: bytes per computed pair from the
+    committed ncu capture summaries (profiles/dram_traffic.json), times this launch's computed pairs;
+    for the tensor-core K loop (3d > 128) per pair and per padded K. None without a capture."""
     p = ROOT / "profiles" / "dram_traffic.json"
     if not p.exists():
         return None
-    rec = json.loads(p.read_text()).get(backend)
-    if not rec:
-        return None
-    return rec["bytes_per_pair"] * pairs
+    table = json.loads(p.read_text())
+    if backend == "bf16" and 3 * d > 128:
+        rec = table.get("bf16_kloop")
+        return rec["bytes_per_pair_per_k"] * ((3 * d + 63) // 64 * 64) * pairs if rec else None
+    rec = table.get(backend)
+    return rec["bytes_per_pair"] * pairs if rec else None
 
 
 def dist_env():
@@ -379,7 +381,7 @@ def main():
             kernel = "k_coarse_fp32 (FP32 tiles + top-(k+m) selection)"
             peak_kind = "derived FP32-FFMA peak at max SM clock"
         achieved = flops / (kms * 1e-3) / 1e12
-        traffic = traffic_per_launch(args.backend, pairs)
+        traffic = traffic_per_launch(args.backend, pairs, d)
         line = {
             "metric": METRIC,
             "value": ws * n / (ms * 1e-3),
