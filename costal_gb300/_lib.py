@@ -97,6 +97,7 @@ U64, U32, I32, INT, DBL, SZ, STR = C.c_uint64, C.c_uint32, C.c_int32, C.c_int, C
 # name -> argtypes (every entry point returns int except costal_version)
 SIGNATURES = {
     "costal_device_ok": [STR, SZ],
+    "costal_check_f64_conversion": [P, STR, SZ],
     "costal_row_l2_norms": [P, U64, U32, P, STR, SZ],
     "costal_knn_exact": [P, U64, U32, U32, P, P, P, P, P, STR, SZ],
     "costal_knn_exact_device": [P, U64, U32, U32, P, P, P, P, P, P, STR, SZ],

@@ -51,6 +51,7 @@ struct Misc {  // small device-side results read back at the end of a call
     unsigned long long blocks_skipped;
     unsigned long long timeout_flag;
     unsigned long long blocks_stopped;
+    unsigned long long conv_mismatches;
 };
 
 struct Context {
@@ -394,6 +395,19 @@ unsigned long long costal_launch_count(void) { return g_launches.load(std::memor
 
 int costal_device_ok(char* err, size_t errlen) {
     return guarded(err, errlen, [](Context&) {});
+}
+
+int costal_check_f64_conversion(uint64_t* mismatches, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        cudaStream_t s = c.stream;
+        CK(ensure(c.misc, sizeof(Misc)));
+        Misc* dm = c.misc.as<Misc>();
+        CK(cudaMemsetAsync(&dm->conv_mismatches, 0, 8, s));
+        CK(launch_check_f64_of(&dm->conv_mismatches, c.sm_count, s));
+        CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        *mismatches = c.h_misc->conv_mismatches;
+    });
 }
 
 int costal_row_l2_norms(const float* x, uint64_t n, uint32_t d, float* out, char* err, size_t errlen) {

@@ -506,10 +506,11 @@ cudaError_t launch_any(const float* xsT, int n, int np, int dp, int cap, int lst
 #undef COSTAL_ARGS
 }
 
-// One warp per listed row: the union of its segments' lists (segs · cap ≤ 256 entries) sorted as
-// (score desc, index asc) keys; the best cap go to the row's candidates, and τ is the cap-th score
-// (≥ every segment's own τ, since a full segment list holds cap entries at or above it), or the
-// row's floor when the segments hold fewer than cap together.
+// One warp per listed row: the union of its segments' lists (segs · cap entries) as (score desc,
+// index asc) keys, 256 at a time: after each warp sort the first cap positions hold the best so far
+// and the other 256 − cap take the next entries. The best cap go to the row's candidates, and τ is
+// the cap-th score (≥ every segment's own τ, since a full segment list holds cap entries at or above
+// it), or the row's floor when the segments hold fewer than cap together.
 __global__ void k_merge_parts(const uint32_t* __restrict__ qlist, int count, int segs, int cap,
                               const uint32_t* __restrict__ part_idx, const float* __restrict__ part_score,
                               const float* __restrict__ tfloor, int lstride, uint32_t* __restrict__ cand_idx,
@@ -517,17 +518,24 @@ __global__ void k_merge_parts(const uint32_t* __restrict__ qlist, int count, int
     const int lane = threadIdx.x & 31;
     const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (r >= count) return;
+    const int total = segs * cap;
+    auto load = [&](int e) {
+        if (e >= total) return PAD_KEY;
+        const size_t o = ((size_t)(e / cap) * count + r) * cap + e % cap;
+        return order_key(part_score[o], part_idx[o]);
+    };
     uint64_t key[8];
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const int e = s * 32 + lane;
-        key[s] = PAD_KEY;
-        if (e < segs * cap) {
-            const size_t o = ((size_t)(e / cap) * count + r) * cap + e % cap;
-            key[s] = order_key(part_score[o], part_idx[o]);
-        }
-    }
+    for (int s = 0; s < 8; ++s) key[s] = load(s * 32 + lane);
     warp_sort_keys<8>(key, lane);
+    for (int next = 256; next < total; next += 256 - cap) {  // warp-uniform
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int p = s * 32 + lane;
+            if (p >= cap) key[s] = load(next + p - cap);
+        }
+        warp_sort_keys<8>(key, lane);
+    }
     const uint32_t q = qlist[r];
     uint64_t kth = 0;
 #pragma unroll
@@ -560,9 +568,10 @@ cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap,
 }
 
 int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
+    // enough CTAs for two per SM; the merge reads segs · cap entries per row, 256 − cap at a time
     const int qblocks = (count + plain::BM - 1) / plain::BM, all = np / plain::BN;
     int segs = (2 * sm_count + qblocks - 1) / qblocks;
-    segs = std::min(segs, 256 / cap);
+    segs = std::min(segs, 64);
     segs = std::min(segs, all / 2);
     if (segs <= 1) return 1;
     const int tps = (all + segs - 1) / segs;

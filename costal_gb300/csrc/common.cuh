@@ -17,10 +17,34 @@ void note_launch();
 // Each helper names the rounding of every operation, so nvcc can never contract a multiply and an
 // add into one FMA where the reference (Rust, which never contracts) rounds twice.
 
+// The exact f64 value of a finite f32, built with integer operations. f32 → f64 is exact, so this is
+// the same value as the conversion instruction; it is written out because the conversion issues to
+// the FP64 pipe, which the GB300 has only a narrow one of, and the rescoring's dot products would
+// otherwise spend two conversions per multiply-add there. Normal numbers move their exponent from
+// bias 127 to bias 1023 (+896 = 0x380) and their 23-bit significand to the top of the 52-bit one;
+// zero keeps its sign; a subnormal m·2⁻¹⁴⁹ is normalised from its leading bit. Not for inf/NaN
+// (the path's inputs are checked finite).
+__device__ __forceinline__ double f64_of(float f) {
+    const uint32_t u = __float_as_uint(f), v = u & 0x7fffffffu, sgn = u & 0x80000000u;
+    uint32_t hi = sgn | ((v >> 3) + 0x38000000u), lo = v << 29;
+    if (v < 0x00800000u) {
+        if (v == 0u) {
+            hi = sgn;
+        } else {  // subnormal: leading bit p in [0, 22], value 2^(p−149)·(1.f)
+            const int p = 31 - __clz(v);
+            const unsigned long long b = ((unsigned long long)(p + 874) << 52) |
+                                         (((unsigned long long)v << (52 - p)) & 0x000fffffffffffffull);
+            hi = sgn | (uint32_t)(b >> 32);
+            lo = (uint32_t)b;
+        }
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 // knn.rs:290-296 `dot64`: Σ_t f64(a_t)·f64(b_t) in dimension order. An f32×f32 product is exact
 // in f64, so fma(a, b, s) rounds exactly like s + a·b: the FMA is bit-identical here.
 __device__ __forceinline__ double dot64_step(double s, float a, float b) {
-    return __fma_rn((double)a, (double)b, s);
+    return __fma_rn(f64_of(a), f64_of(b), s);
 }
 
 // knn.rs:301-312 `cos64`: 0 for a zero row, dot / (n_i·n_j), −0 → +0.

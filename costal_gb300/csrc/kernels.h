@@ -31,6 +31,8 @@ cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, in
 cudaError_t launch_rerun_floor(const uint32_t* rows, const unsigned* count, int nmax, int cap, const float* tau,
                                const float* cand_score, const double* row_eps, double eps, float* tfloor,
                                cudaStream_t st);
+// Self-check of the integer f32 → f64 conversion used by the f64 dot products (all 2³² patterns).
+cudaError_t launch_check_f64_of(unsigned long long* mismatches, int sm_count, cudaStream_t st);
 cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lstride, const uint32_t* cand_idx,
                            const float* cand_score, const float* tau, const double* norms, const double* row_eps,
                            const double* row_ub, unsigned* ub_fail, double eps, int certify, int select,

@@ -167,10 +167,33 @@ __device__ __forceinline__ void warp_sort(double (&sc)[SLOTS], double (&cs)[SLOT
     }
 }
 
-// Two phases per CTA of 8 rows. (1) Every thread rescores candidates of the flattened (row, slot)
-// list — all lanes busy whatever cap is, since the f64 dot products are the kernel's cost on the
-// GB300's narrow FP64 pipe — into shared memory. (2) One warp per row sorts its cap results,
-// certifies and writes the row.
+// The k-th largest of a warp's 32·SLOTS order keys (ballot counts, bit by bit from the top).
+template <int SLOTS>
+__device__ __forceinline__ uint32_t warp_kth_key(const uint32_t (&key)[SLOTS], int k) {
+    uint32_t prefix = 0;
+    int need = k;
+#pragma unroll 1
+    for (int b = 31; b >= 0; --b) {
+        const uint32_t hmask = ~0u << b, want = prefix | (1u << b);
+        int c = 0;
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) c += __popc(__ballot_sync(COSTAL_FULL_MASK, (key[s] & hmask) == want));
+        if (c >= need) prefix = want;
+        else need -= c;
+    }
+    return prefix;
+}
+
+// Three phases per CTA of 8 rows.
+// (0) One warp per row finds the k-th largest coarse score c_k among the row's candidates. At least k
+//     candidates score ≥ c_k coarse, so ≥ c_k − E exact, so the row's exact k-th score s_k ≥ c_k − E;
+//     a candidate whose coarse score is below c_k − 2E scores below s_k exactly and can neither enter
+//     the top-k nor change s_k. Only the others are rescored (cosine selection; E the row's coarse
+//     error bound); they are packed into one list for the CTA.
+// (1) Every thread rescores entries of that list — all lanes of a warp on real work, since the f64
+//     dot products are the kernel's cost on the GB300's narrow FP64 pipe — into shared memory.
+// (2) One warp per row sorts its cap results (skipped and empty slots as −∞), certifies and writes
+//     the row.
 constexpr int RS_ROWS = 8;
 constexpr int RS_MAXCAP = 128;
 
@@ -186,7 +209,8 @@ __global__ void __launch_bounds__(256)
               unsigned* __restrict__ fb_count, unsigned long long* __restrict__ max_err_bits) {
     __shared__ double sc_s[RS_ROWS * RS_MAXCAP], cs_s[RS_ROWS * RS_MAXCAP];
     __shared__ uint32_t id_s[RS_ROWS * RS_MAXCAP];
-    __shared__ int row_s[RS_ROWS];
+    __shared__ uint16_t work_s[RS_ROWS * RS_MAXCAP];  // packed (row, slot) entries to rescore
+    __shared__ int row_s[RS_ROWS], cnt_s[RS_ROWS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nrows = rlist ? (int)*rcount : n;
     const int w0 = blockIdx.x * RS_ROWS;
@@ -194,41 +218,96 @@ __global__ void __launch_bounds__(256)
     const int nr = min(RS_ROWS, nrows - w0);
     if (tid < RS_ROWS) row_s[tid] = tid < nr ? (rlist ? (int)rlist[w0 + tid] : w0 + tid) : 0;
     __syncthreads();
+    // phase 0: which slots need the f64 score
+    unsigned keep[SLOTS] = {};
+    if (warp < nr) {
+        const int i = row_s[warp];
+        uint32_t key[SLOTS];
+        int valid = 0;
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) {
+            const int p = s * 32 + lane;
+            key[s] = 0;  // below every real score's key
+            if (p < cap && cand_idx[(size_t)i * lstride + p] < (uint32_t)n) {
+                const uint32_t u = __float_as_uint(cand_score[(size_t)i * lstride + p]);
+                key[s] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+            }
+            valid += __popc(__ballot_sync(COSTAL_FULL_MASK, key[s] != 0));
+        }
+        double thr = -CUDART_INF;
+        if (select == 0 && valid >= k) {
+            const uint32_t h = warp_kth_key<SLOTS>(key, k);
+            const float ck = __uint_as_float((h & 0x80000000u) ? (h & 0x7fffffffu) : ~h);
+            const double e = row_eps ? row_eps[i] : eps;
+            thr = __dsub_rd((double)ck, __dadd_ru(e, e));
+        }
+        int n_keep = 0;
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) {
+            const int p = s * 32 + lane;
+            bool kp = false;
+            if (key[s] != 0) {
+                const float cf = __uint_as_float((key[s] & 0x80000000u) ? (key[s] & 0x7fffffffu) : ~key[s]);
+                kp = !((double)cf < thr);
+            }
+            keep[s] = __ballot_sync(COSTAL_FULL_MASK, kp);
+            if (!kp && p < cap) {
+                sc_s[warp * cap + p] = -CUDART_INF;
+                cs_s[warp * cap + p] = 0.0;
+                id_s[warp * cap + p] = 0xffffffffu;
+            }
+            n_keep += __popc(keep[s]);
+        }
+        if (lane == 0) cnt_s[warp] = n_keep;
+    } else if (lane == 0) {
+        cnt_s[warp] = 0;  // (blockDim = 32·RS_ROWS: one warp per row slot)
+    }
+    __syncthreads();
+    int total = 0, base = 0;
+#pragma unroll
+    for (int r = 0; r < RS_ROWS; ++r) {
+        base += r < warp ? cnt_s[r] : 0;
+        total += cnt_s[r];
+    }
+    if (warp < nr) {
+        int off = base;
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) {
+            if (keep[s] >> lane & 1u)
+                work_s[off + __popc(keep[s] & ((1u << lane) - 1u))] = (uint16_t)(warp * RS_MAXCAP + s * 32 + lane);
+            off += __popc(keep[s]);
+        }
+    }
+    __syncthreads();
+    // phase 1: the f64 rescoring of the packed entries
     const bool vec4 = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
     double err = 0.0;
-    for (int e = tid; e < nr * cap; e += blockDim.x) {
-        const int r = e / cap, p = e - r * cap;
+    for (int w = tid; w < total; w += blockDim.x) {
+        const int code = work_s[w], r = code / RS_MAXCAP, p = code - r * RS_MAXCAP, e = r * cap + p;
         const int i = row_s[r];
         const uint32_t j = cand_idx[(size_t)i * lstride + p];
-        if (j < (uint32_t)n) {
-            // (an index ≥ n marks an empty slot: the coarse pass kept fewer than cap candidates)
-            const float* xi = x + (size_t)i * d;
-            const float* xj = x + (size_t)j * d;
-            double dot = 0.0;
-            if (vec4) {  // the same dimension order, 16-byte loads
-                for (int t = 0; t < d; t += 4) {
-                    const float4 a = __ldg(reinterpret_cast<const float4*>(xi + t));
-                    const float4 b = __ldg(reinterpret_cast<const float4*>(xj + t));
-                    dot = dot64_step(dot, a.x, b.x);
-                    dot = dot64_step(dot, a.y, b.y);
-                    dot = dot64_step(dot, a.z, b.z);
-                    dot = dot64_step(dot, a.w, b.w);
-                }
-            } else {
-                for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
+        const float* xi = x + (size_t)i * d;
+        const float* xj = x + (size_t)j * d;
+        double dot = 0.0;
+        if (vec4) {  // the same dimension order, 16-byte loads
+            for (int t = 0; t < d; t += 4) {
+                const float4 a = __ldg(reinterpret_cast<const float4*>(xi + t));
+                const float4 b = __ldg(reinterpret_cast<const float4*>(xj + t));
+                dot = dot64_step(dot, a.x, b.x);
+                dot = dot64_step(dot, a.y, b.y);
+                dot = dot64_step(dot, a.z, b.z);
+                dot = dot64_step(dot, a.w, b.w);
             }
-            const double ni = norms[i], nj = norms[j];
-            const double c = cos64(dot, ni, nj);
-            const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
-            err = fmax(err, fabs((double)cand_score[(size_t)i * lstride + p] - score));
-            sc_s[e] = score;
-            cs_s[e] = c;
-            id_s[e] = j;
         } else {
-            sc_s[e] = -CUDART_INF;
-            cs_s[e] = 0.0;
-            id_s[e] = 0xffffffffu;
+            for (int t = 0; t < d; ++t) dot = dot64_step(dot, __ldg(xi + t), __ldg(xj + t));
         }
+        const double ni = norms[i], nj = norms[j];
+        const double c = cos64(dot, ni, nj);
+        const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
+        err = fmax(err, fabs((double)cand_score[(size_t)i * lstride + p] - score));
+        sc_s[e] = score;
+        cs_s[e] = c;
+        id_s[e] = j;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
@@ -391,6 +470,24 @@ cudaError_t launch_prep(const float* x, int n, int d, int np, int dp, double* no
 
 cudaError_t launch_row_l2_norms_f32(const float* x, int n, int d, float* out, cudaStream_t st) {
     k_row_l2_norms_f32<<<(n + 255) / 256, 256, 0, st>>>(x, n, d, out); note_launch();
+    return cudaGetLastError();
+}
+
+// Every finite f32 bit pattern: f64_of against the conversion instruction; counts the mismatches.
+__global__ void k_check_f64_of(unsigned long long* __restrict__ mismatches) {
+    unsigned long long bad = 0;
+    for (unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; b < (1ull << 32);
+         b += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t u = (uint32_t)b;
+        if ((u & 0x7f800000u) == 0x7f800000u) continue;  // inf / NaN
+        const float f = __uint_as_float(u);
+        bad += __double_as_longlong(f64_of(f)) != __double_as_longlong((double)f);
+    }
+    if (bad) atomicAdd(mismatches, bad);
+}
+
+cudaError_t launch_check_f64_of(unsigned long long* mismatches, int sm_count, cudaStream_t st) {
+    k_check_f64_of<<<8 * sm_count, 256, 0, st>>>(mismatches); note_launch();
     return cudaGetLastError();
 }
 

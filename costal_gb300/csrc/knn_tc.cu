@@ -4,11 +4,15 @@
 // threshold scan and per-row heaps), with the dot products on the tensor cores:
 //
 //   split     Every normalised row a (f32) is written as a = a_hi + a_lo + r with a_hi = bf16(a),
-//             a_lo = bf16(a − a_hi); |r| ≤ 2⁻¹⁶|a|. The query operand is A = [a_hi | a_lo | a_hi] and
-//             the column operand B = [b_hi | b_hi | b_lo] (K = 3d, zero-padded to a multiple of 64), so
-//             ONE tcgen05.mma chain computes a_hi·b_hi + a_lo·b_hi + a_hi·b_lo with FP32 accumulation
-//             in TMEM. Plain BF16 would put ~2⁻⁸ of error on every cosine, far wider than the gap
-//             between the k-th and (k+m)-th neighbour; the split keeps the bound near 5e-5.
+//             a_lo = bf16(a − a_hi); |r| ≤ 2⁻¹⁶|a|. The tensor cores compute a_hi·b_hi + a_lo·b_hi +
+//             a_hi·b_lo with FP32 accumulation in TMEM. Plain BF16 would put ~2⁻⁸ of error on every
+//             cosine, far wider than the gap between the k-th and (k+m)-th neighbour; the split keeps
+//             the bound near 5e-5. Usually A = [a_hi | a_lo | a_hi], B = [b_hi | b_hi | b_lo] (K = 3d,
+//             zero-padded to a multiple of 64) and one MMA chain; the query tile stays resident for
+//             3d ≤ 128, deeper rows stream both operands by K block. Compact operands (22 ≤ d ≤ 32,
+//             where they save a column K block): A = [a_hi | a_hi | 0 | a_lo | 0] resident, a column
+//             row is only B = [b_hi | b_lo] (2d bf16), and two chains run into one accumulator: A's
+//             [hi | hi] × B's [hi | lo], then A's [lo] × B's leading [hi].
 //   kernel    One CTA per 128 query rows (M = 128, one TMEM lane per query), column tiles of N = 256.
 //             Warp 4 streams B tiles with TMA (128-byte swizzle) into a ring of shared-memory
 //             stages; warp 5 issues the MMAs (one elected thread) into two 256-column TMEM
@@ -28,6 +32,8 @@
 //
 // Every mbarrier wait is bounded: after 2²² polls a thread raises `timeout_flag` and its role stops
 // (and every other wait of the launch then returns at once); the host reports COSTAL_ETIMEOUT.
+
+#include <algorithm>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -376,7 +382,7 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
 template <int SLOTS, bool KLOOP>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
-                int nkb, int ksteps, int stages, int cap, const uint32_t* __restrict__ perm,
+                int nkb, int nkb_b, int ksteps, int k1s, int stages, int cap, const uint32_t* __restrict__ perm,
                 const uint32_t* __restrict__ lists, const float* __restrict__ list_ub,
                 const uint32_t* __restrict__ counts, int ncb, const double* __restrict__ row_eps,
                 uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
@@ -387,10 +393,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // 1024-byte alignment for the swizzled tiles
     const uint32_t base_u32 = smem_u32(smem_raw);
     unsigned char* smem = smem_raw + ((1024 - (base_u32 & 1023)) & 1023);
-    // Resident A: the query tile (nkb K blocks) once, then `stages` column tiles of nkb K blocks.
-    // K loop (deep rows, KLOOP): every stage holds one K block of the query tile and of the column
-    // tile, and a tile's MMA chain runs over nkb stages.
-    const uint32_t stage_bytes = KLOOP ? (uint32_t)(A_KB_BYTES + B_KB_BYTES) : (uint32_t)nkb * B_KB_BYTES;
+    // Resident A: the query tile (nkb K blocks) once, then `stages` column tiles of nkb_b K blocks. K loop (deep rows, KLOOP): every stage holds one K block of the query tile
+    // and of the column tile, and a tile's MMA chain runs over nkb stages.
+    const uint32_t stage_bytes = KLOOP ? (uint32_t)(A_KB_BYTES + B_KB_BYTES) : (uint32_t)nkb_b * B_KB_BYTES;
     unsigned char* a_tile = smem;                                            // nkb × 16 KB (resident A)
     unsigned char* b_tiles = KLOOP ? smem : a_tile + (size_t)nkb * A_KB_BYTES;  // stages × stage_bytes
     float* B_s = reinterpret_cast<float*>(b_tiles + (size_t)stages * stage_bytes);  // [BCAP][BSTRIDE]
@@ -404,7 +409,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int ntiles = lists ? (int)counts[blockIdx.x] : np / BLOCK_N;
     const uint32_t* my_list = lists ? lists + (size_t)blockIdx.x * ncb : nullptr;
     auto block_of = [&](int t) -> int { return my_list ? (int)my_list[t] : t; };
-    const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb * B_KB_BYTES;
+    const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb_b * B_KB_BYTES;
     (void)a_bytes;
 
     if (threadIdx.x == 0) {
@@ -506,7 +511,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 mbar_expect_tx(&bars->b_full[s], b_bytes);
                 unsigned char* dst = b_tiles + (size_t)s * b_bytes;
                 const int cb = block_of(t) * BLOCK_N;
-                for (int kb = 0; kb < nkb; ++kb) tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
+                // (the last K block may reach past the operand's row: TMA fills those columns with zeros
+                // and reads nothing for them)
+                for (int kb = 0; kb < nkb_b; ++kb)
+                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
             }
         }
     } else if (warp == EPI_WARPS + 1) {
@@ -560,10 +568,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 const uint32_t b_base = smem_u32(b_tiles + (size_t)s * b_bytes);
                 const uint32_t d = tmem + (uint32_t)(buf * BLOCK_N);
+                // Two chains into one accumulator: steps [0, k1s) pair A's [hi | hi] with B's [hi | lo];
+                // steps [k1s, ksteps) pair A's [lo] with B's leading [hi] (A's zero padding cancels
+                // whatever of B's lo those steps also cover). 16 bf16 = 32 bytes inside a swizzle row.
                 for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint32_t koff = (uint32_t)((ks & 3) * 32);  // 16 bf16 = 32 bytes inside the swizzle row
-                    const uint64_t ad = sw128_desc(a_base + (uint32_t)(ks >> 2) * A_KB_BYTES + koff);
-                    const uint64_t bd = sw128_desc(b_base + (uint32_t)(ks >> 2) * B_KB_BYTES + koff);
+                    const int kb = ks < k1s ? ks : ks - k1s;
+                    const uint64_t ad = sw128_desc(a_base + (uint32_t)(ks >> 2) * A_KB_BYTES + (uint32_t)((ks & 3) * 32));
+                    const uint64_t bd = sw128_desc(b_base + (uint32_t)(kb >> 2) * B_KB_BYTES + (uint32_t)((kb & 3) * 32));
                     mma_bf16(d, ad, bd, ks > 0 ? 1u : 0u);
                 }
                 mma_commit(&bars->b_empty[s]);
@@ -705,23 +716,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // into the two operands in shared memory and records the f64 norms of the pieces: [0] ‖a_hi‖,
 // [1] ‖a_lo‖, [2] ‖r‖, [3] ‖a_hi + a_lo‖; then the CTA writes the 128 operand rows with coalesced
 // word stores. Rows in [n, rows) are written as zeros. The maxima over rows go to colmax through one
-// atomic per warp.
+// atomic per warp. Two layouts: compact (k1 > 0) A = [hi | hi | 0 … k1 | lo | 0 … kpa] and
+// B = [hi | lo | 0 … kpb]; otherwise A = [hi | lo | hi | 0 … kp], B = [hi | hi | lo | 0 … kp].
 constexpr int SPLIT_ROWS = 128;
 __global__ void __launch_bounds__(SPLIT_ROWS)
-    k_split(const float* __restrict__ xsT, int n, int np_x, int rows, int d, int kp, const uint32_t* __restrict__ perm,
-            __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm,
-            unsigned long long* __restrict__ colmax) {
-    extern __shared__ uint32_t sw[];  // [2][SPLIT_ROWS][kp/2 + 1] words of bf16 pairs
-    const int ws = kp / 2 + 1;        // odd word stride: the 32 lanes' rows fall in 32 banks
+    k_split(const float* __restrict__ xsT, int n, int np_x, int rows, int d, int kpa, int kpb, int k1,
+            const uint32_t* __restrict__ perm, __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb,
+            double* __restrict__ pnorm, unsigned long long* __restrict__ colmax) {
+    extern __shared__ uint32_t sw[];  // [SPLIT_ROWS][kpa/2 + 1] then [SPLIT_ROWS][kpb/2 + 1] words
+    const int wsa = kpa / 2 + 1, wsb = kpb / 2 + 1;  // odd word strides: the 32 lanes' rows fall in 32 banks
     __nv_bfloat16* ta = reinterpret_cast<__nv_bfloat16*>(sw);
-    __nv_bfloat16* tb = reinterpret_cast<__nv_bfloat16*>(sw + SPLIT_ROWS * ws);
+    __nv_bfloat16* tb = reinterpret_cast<__nv_bfloat16*>(sw + SPLIT_ROWS * wsa);
     const int lr = threadIdx.x, r = blockIdx.x * SPLIT_ROWS + lr;  // working row
     const bool live = r < n;
     const int o = live ? (perm ? (int)perm[r] : r) : 0;  // its original row
-    __nv_bfloat16* ra = ta + (size_t)lr * 2 * ws;
-    __nv_bfloat16* rb = tb + (size_t)lr * 2 * ws;
+    __nv_bfloat16* ra = ta + (size_t)lr * 2 * wsa;
+    __nv_bfloat16* rb = tb + (size_t)lr * 2 * wsb;
     double sh = 0.0, sl = 0.0, sr = 0.0, sp = 0.0;
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
+    for (int t = 0; t < kpa; ++t) ra[t] = zero;
+    for (int t = 0; t < kpb; ++t) rb[t] = zero;
     for (int t = 0; t < d; ++t) {
         const float a = live ? xsT[(size_t)t * np_x + o] : 0.0f;
         const __nv_bfloat16 hb = __float2bfloat16_rn(a);
@@ -730,21 +744,25 @@ __global__ void __launch_bounds__(SPLIT_ROWS)
         const __nv_bfloat16 lb = __float2bfloat16_rn(e);
         const float l = __bfloat162float(lb);
         const float rem = e - l;  // exact in f32
-        ra[t] = hb;
-        ra[d + t] = lb;
-        ra[2 * d + t] = hb;
-        rb[t] = hb;
-        rb[d + t] = hb;
-        rb[2 * d + t] = lb;
+        if (k1 > 0) {
+            ra[t] = hb;
+            ra[d + t] = hb;
+            ra[k1 + t] = lb;
+            rb[t] = hb;
+            rb[d + t] = lb;
+        } else {
+            ra[t] = hb;
+            ra[d + t] = lb;
+            ra[2 * d + t] = hb;
+            rb[t] = hb;
+            rb[d + t] = hb;
+            rb[2 * d + t] = lb;
+        }
         sh = __fma_rn((double)h, (double)h, sh);
         sl = __fma_rn((double)l, (double)l, sl);
         sr = __fma_rn((double)rem, (double)rem, sr);
         const double p = (double)h + (double)l;
         sp = __fma_rn(p, p, sp);
-    }
-    for (int t = 3 * d; t < kp; ++t) {
-        ra[t] = zero;
-        rb[t] = zero;
     }
     const double v[4] = {sqrt(sh), sqrt(sl), sqrt(sr), sqrt(sp)};
 #pragma unroll
@@ -761,15 +779,16 @@ __global__ void __launch_bounds__(SPLIT_ROWS)
             atomicMax(&colmax[j], b);
     }
     __syncthreads();
-    const int wpr = kp / 2;  // words per operand row
-    uint32_t* ga = reinterpret_cast<uint32_t*>(opa) + (size_t)blockIdx.x * SPLIT_ROWS * wpr;
-    uint32_t* gb = reinterpret_cast<uint32_t*>(opb) + (size_t)blockIdx.x * SPLIT_ROWS * wpr;
-    for (int e = threadIdx.x; e < SPLIT_ROWS * wpr; e += SPLIT_ROWS) {
-        const int row = e / wpr, w = e % wpr;
-        if (blockIdx.x * SPLIT_ROWS + row < rows) {
-            ga[e] = sw[row * ws + w];
-            gb[e] = sw[SPLIT_ROWS * ws + row * ws + w];
-        }
+    const int wpa = kpa / 2, wpb = kpb / 2;  // words per operand row
+    uint32_t* ga = reinterpret_cast<uint32_t*>(opa) + (size_t)blockIdx.x * SPLIT_ROWS * wpa;
+    uint32_t* gb = reinterpret_cast<uint32_t*>(opb) + (size_t)blockIdx.x * SPLIT_ROWS * wpb;
+    for (int e = threadIdx.x; e < SPLIT_ROWS * wpa; e += SPLIT_ROWS) {
+        const int row = e / wpa, w = e % wpa;
+        if (blockIdx.x * SPLIT_ROWS + row < rows) ga[e] = sw[row * wsa + w];
+    }
+    for (int e = threadIdx.x; e < SPLIT_ROWS * wpb; e += SPLIT_ROWS) {
+        const int row = e / wpb, w = e % wpb;
+        if (blockIdx.x * SPLIT_ROWS + row < rows) gb[e] = sw[SPLIT_ROWS * wsa + row * wsb + w];
     }
 }
 
@@ -849,27 +868,66 @@ __global__ void k_row_eps(const double* __restrict__ pnorm, const unsigned long 
 
 static int kpad(int d) { return (3 * d + KB - 1) / KB * KB; }
 
-// Up to two K blocks (3d ≤ 128) the query tile stays resident; deeper rows run the K loop.
-static bool kloop(int nkb) { return nkb > 2; }
-
-static size_t fixed_smem(int nkb, int cap) {
-    const int bcap = cap <= 32 ? 64 : 128;
-    return 1024 + (kloop(nkb) ? 0 : (size_t)nkb * A_KB_BYTES) + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
+// The operand shape for d. Three forms:
+//   resident, 3d-wide (3d ≤ 128): A = [hi | lo | hi] stays in shared memory for the whole CTA, each
+//     stage holds one column tile B = [hi | hi | lo], one MMA chain;
+//   resident, compact (when it needs fewer column K blocks than the 3d-wide form, 22 ≤ d ≤ 32):
+//     A = [hi | hi | 0 | lo | 0] resident, a column row is only B = [hi | lo] (2d bf16, ≥ 64), two
+//     chains into one accumulator — the column tile, streamed for every tile, is one K block;
+//   K loop (3d > 128): both 3d-wide operands streamed one K block per stage.
+struct Shape {
+    bool resident;  // the query tile stays in shared memory (else the K loop)
+    bool compact;   // [hi | hi | lo] × [hi | lo] operands (else [hi | lo | hi] × [hi | hi | lo])
+    int kpa, kpb;   // operand row lengths (bf16) of A and B
+    int nkb_a;      // K blocks of A (resident) or of both operands (K loop)
+    int nkb_b;      // K blocks of B per stage (resident)
+    int ksteps;     // MMA steps of 16 per tile
+    int k1s;        // steps of the first chain (compact: A [hi | hi] × B [hi | lo]; else all of them)
+    int keff;       // products per dot product, for the accumulation term of the bound
+};
+static Shape shape_of(int d) {
+    Shape s{};
+    const int kp = kpad(d);
+    const int k1 = (2 * d + 15) / 16 * 16, k2 = (d + 15) / 16 * 16;
+    if (k1 + k2 <= 2 * KB && (k1 + KB - 1) / KB < kp / KB) {
+        s.resident = s.compact = true;
+        s.kpa = (k1 + k2 + KB - 1) / KB * KB;
+        s.kpb = std::max(KB, (2 * d + 7) / 8 * 8);
+        s.nkb_a = s.kpa / KB;
+        s.nkb_b = (k1 + KB - 1) / KB;
+        s.ksteps = (k1 + k2) / 16;
+        s.k1s = k1 / 16;
+        s.keff = k1 + k2;
+    } else {
+        s.resident = kp <= 2 * KB;
+        s.compact = false;
+        s.kpa = s.kpb = kp;
+        s.nkb_a = s.nkb_b = kp / KB;
+        s.ksteps = (3 * d + 15) / 16;
+        s.k1s = s.ksteps;
+        s.keff = 3 * d;
+    }
+    return s;
 }
-static size_t stage_smem(int nkb) {
-    return kloop(nkb) ? (size_t)(A_KB_BYTES + B_KB_BYTES) : (size_t)nkb * B_KB_BYTES;
+
+static size_t fixed_smem(const Shape& sh, int cap) {
+    const int bcap = cap <= 32 ? 64 : 128;
+    return 1024 + (sh.resident ? (size_t)sh.nkb_a * A_KB_BYTES : 0) + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
+}
+static size_t stage_smem(const Shape& sh) {
+    return sh.resident ? (size_t)sh.nkb_b * B_KB_BYTES : (size_t)(A_KB_BYTES + B_KB_BYTES);
 }
 
 bool supported(int d, int cap) {
     if (d < 1 || cap < 1 || cap > 64) return false;
-    const int nkb = kpad(d) / KB;
-    return fixed_smem(nkb, cap) + stage_smem(nkb) <= 227 * 1024;  // at least one stage
+    const Shape sh = shape_of(d);
+    return fixed_smem(sh, cap) + stage_smem(sh) <= 227 * 1024;  // at least one stage
 }
 
 size_t workspace_bytes(int n, int d) {
     const size_t np = (size_t)(n + 255) / 256 * 256;
-    const size_t kp = (size_t)kpad(d);
-    return 2 * np * kp * 2 + 4 * (size_t)n * 8 + (size_t)n * 8 + 4 * 8 + 4096;
+    const Shape sh = shape_of(d);
+    return np * (size_t)(sh.kpa + sh.kpb) * 2 + 4 * (size_t)n * 8 + (size_t)n * 8 + 4 * 8 + 4096;
 }
 
 namespace {
@@ -904,13 +962,14 @@ struct Layout {
 };
 
 Layout carve(void* ws, int n, int d) {
-    const size_t np = (size_t)(n + 255) / 256 * 256, kp = (size_t)kpad(d);
+    const size_t np = (size_t)(n + 255) / 256 * 256;
+    const Shape sh = shape_of(d);
     char* p = static_cast<char*>(ws);
     Layout L;
     L.opa = reinterpret_cast<__nv_bfloat16*>(p);
-    p += np * kp * 2;
+    p += np * (size_t)sh.kpa * 2;
     L.opb = reinterpret_cast<__nv_bfloat16*>(p);
-    p += np * kp * 2;
+    p += np * (size_t)sh.kpb * 2;
     L.pnorm = reinterpret_cast<double*>(p);
     p += 4 * (size_t)n * 8;
     L.row_eps = reinterpret_cast<double*>(p);
@@ -924,26 +983,28 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
                     Plan& plan) {
     (void)dp;
     const int np = (n + 255) / 256 * 256;  // the tensor tiles are 256 columns wide
-    const int kp = kpad(d);
+    const Shape sh = shape_of(d);
     Layout L = carve(ws, n, d);
     cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
     if (e != cudaSuccess) return e;
     // xsT has ⌈n/128⌉·128 columns; operand rows in [n, np) are zero-filled by k_split itself.
-    const size_t smem = (size_t)2 * SPLIT_ROWS * (kp / 2 + 1) * 4;
+    const size_t smem = (size_t)SPLIT_ROWS * (sh.kpa / 2 + 1 + sh.kpb / 2 + 1) * 4;
     if (smem <= 227 * 1024) {
         e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, kp, perm, L.opa, L.opb, L.pnorm,
-                                                            L.colmax);
-    } else {
-        k_split_wide<<<np, 256, 0, st>>>(xsT, n, np_x, d, kp, perm, L.opa, L.opb, L.pnorm, L.colmax);
+        k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, sh.kpa, sh.kpb,
+                                                            sh.compact ? sh.k1s * 16 : 0, perm, L.opa, L.opb,
+                                                            L.pnorm, L.colmax);
+    } else {  // (deep rows: never the compact shape)
+        k_split_wide<<<np, 256, 0, st>>>(xsT, n, np_x, d, sh.kpa, perm, L.opa, L.opb, L.pnorm, L.colmax);
     }
     note_launch();
-    k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, 3 * d, L.row_eps); note_launch();
+    k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, sh.keff, L.row_eps); note_launch();
     plan.n = n;
     plan.d = d;
     plan.np = np;
-    plan.kp = kp;
+    plan.kpa = sh.kpa;
+    plan.kpb = sh.kpb;
     plan.ops_a = L.opa;
     plan.ops_b = L.opb;
     plan.row_eps = L.row_eps;
@@ -958,21 +1019,21 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
                           cudaStream_t st) {
     (void)sm_count;
     CUtensorMap ma, mb;
-    if (!make_map(&ma, plan.ops_a, plan.kp, plan.np, BLOCK_M) || !make_map(&mb, plan.ops_b, plan.kp, plan.np, BLOCK_N))
+    if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M) || !make_map(&mb, plan.ops_b, plan.kpb, plan.np, BLOCK_N))
         return cudaErrorInvalidValue;
-    const int nkb = plan.kp / KB;
-    const int ksteps = (3 * plan.d + 15) / 16;
-    const size_t fixed = fixed_smem(nkb, cap), per = stage_smem(nkb);
+    const Shape sh = shape_of(plan.d);
+    const size_t fixed = fixed_smem(sh, cap), per = stage_smem(sh);
     int stages = 4;
     while (stages > 1 && fixed + (size_t)stages * per > 227 * 1024) --stages;
     const size_t smem = fixed + (size_t)stages * per;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
-    auto kern = kloop(nkb) ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
-                           : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
+    auto kern = !sh.resident ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
+                             : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, nkb, ksteps, stages, cap, plan.perm, lists,
+    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages, cap,
+                                          plan.perm, lists,
                                           lists ? list_ub : nullptr, counts, ncb, plan.row_eps, cand_idx, cand_score,
                                           tau, stopped_total, timeout_flag); note_launch();
     return cudaGetLastError();

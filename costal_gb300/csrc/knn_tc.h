@@ -12,9 +12,10 @@ constexpr int BLOCK_M = 128;  // query rows per CTA tile (the MMA's M; one TMEM 
 constexpr int BLOCK_N = 256;  // columns per tile (the MMA's N)
 
 struct Plan {
-    int n, d, np, kp;       // rows, features, padded rows, padded K of the split operands
-    const void* ops_a;      // [np][kp] bf16 query operand   (hi | lo | hi)
-    const void* ops_b;      // [np][kp] bf16 column operand  (hi | hi | lo)
+    int n, d, np;           // rows, features, padded rows
+    int kpa, kpb;           // row lengths (bf16) of the split operands
+    const void* ops_a;      // [np][kpa] bf16 query operand  (hi | hi | lo, or hi | lo | hi for deep rows)
+    const void* ops_b;      // [np][kpb] bf16 column operand (hi | lo, or hi | hi | lo for deep rows)
     const double* row_eps;  // [n] certificate bound of each query row
     const double* col_max;  // [4] maxima over all rows of the split-residual norms
     const uint32_t* perm;   // working -> original row (NULL: identity); operands are in working order

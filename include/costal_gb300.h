@@ -79,6 +79,10 @@ const char* costal_version(void);   /* replaces env!("CARGO_PKG_VERSION") of lib
    in this process (a monotone counter; take differences around a call). */
 unsigned long long costal_launch_count(void);
 int costal_device_ok(char* err, size_t errlen);  /* 0 when a usable sm_103 device is present */
+/* GB300 addition, no reference counterpart: a self-check of the integer f32 -> f64 conversion that
+   the f64 rescoring uses in place of the conversion instruction; compares the two over every finite
+   f32 bit pattern on the device and stores the number of mismatches (0 expected). */
+int costal_check_f64_conversion(uint64_t* mismatches, char* err, size_t errlen);
 /* lib.rs:94-102 (costal_core::row_l2_norms, crates/costal-core/src/lib.rs:34-47): f32 row norms. */
 int costal_row_l2_norms(const float* x, uint64_t n, uint32_t d, float* out, char* err, size_t errlen);
 

@@ -83,6 +83,35 @@ def test_tie_heavy_integer_data_stays_exact(ext, oracle):
     assert stats["fallback_rows"] > 0
 
 
+def test_integer_f64_conversion_matches_the_instruction(ext):
+    """The f64 dot products widen f32 with integer operations; every finite f32 must come out the same."""
+    import ctypes as C
+
+    from costal_gb300 import _lib
+
+    bad = C.c_uint64(99)
+    err, size = _lib.errbuf()
+    _lib.check(_lib.lib().costal_check_f64_conversion(C.addressof(bad), err, size), err)
+    assert bad.value == 0
+
+
+@pytest.mark.parametrize("matmul", ["gemm", "bf16"])
+def test_subnormal_and_signed_zero_entries(ext, oracle, matmul):
+    """Subnormal, ±0 and tiny entries go through the same f64 rescoring bit for bit."""
+    rng = np.random.default_rng(21)
+    x = clustered(900, 24, 4)
+    x[rng.random(x.shape) < 0.15] = np.float32(-0.0)
+    x[rng.random(x.shape) < 0.05] = 0.0
+    sub = (rng.integers(1, 1 << 23, size=x.shape).astype(np.uint32)).view(np.float32)  # subnormal magnitudes
+    sign = np.where(rng.random(x.shape) < 0.5, np.float32(-1), np.float32(1))
+    m = rng.random(x.shape) < 0.1
+    x[m] = (sub * sign)[m]
+    x[7] = (sub[7] * sign[7])  # a row of subnormals only
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    got, _ = ext._knn_exact(x, 9, matmul=matmul)
+    same(as_oracle(got), oracle.knn_bruteforce(x, 9))
+
+
 def test_lcg_known_answers(ext, oracle):
     # knn.rs:1001-1044 on the reference's own generator
     g = Lcg(3)
@@ -115,8 +144,21 @@ def test_shapes_and_margins(ext, oracle, n, d, k, margin):
     same(as_oracle(got), oracle.knn_bruteforce(x, k))
 
 
+@pytest.mark.parametrize("n,d,k,margin", [(900, 1, 6, None), (800, 8, 10, None), (1100, 16, 12, 4), (700, 24, 10, None),
+                                          (1000, 31, 20, 30), (1200, 32, 10, None), (900, 33, 15, None),
+                                          (1300, 39, 10, 10), (1500, 40, 10, None), (600, 40, 30, 30)])
+def test_compact_operands_on_the_tensor_cores(ext, oracle, n, d, k, margin):
+    """Around the compact operand range (22 ≤ d ≤ 32: 2d-wide [hi | lo] column rows, two MMA chains)
+    and the 3d-wide resident form on either side of it."""
+    rng = np.random.default_rng(3 * n + d)
+    means = rng.normal(0, 2, size=(9, d))
+    x = np.arcsinh((means[rng.integers(0, 9, n)] + rng.normal(0, 0.6, size=(n, d))) / 5.0).astype(np.float32)
+    got, st = ext._knn_exact(x, k, margin=margin, matmul="bf16")
+    same(as_oracle(got), oracle.knn_bruteforce(x, k))
+
+
 @pytest.mark.parametrize("n,d,k,margin", [(700, 43, 10, None), (600, 300, 15, None), (500, 2000, 15, 15),
-                                          (400, 130, 20, 40)])
+                                          (400, 130, 20, 40), (650, 41, 10, None), (640, 42, 12, 12)])
 def test_deep_rows_on_the_tensor_cores(ext, oracle, n, d, k, margin):
     """Rows deeper than two K blocks run the tensor-core K loop (no locality order): same exact output."""
     rng = np.random.default_rng(n + d)
