@@ -193,8 +193,8 @@ def main():
     ap.add_argument("--backend", default="bf16", choices=["fp32", "bf16"])
     ap.add_argument("--no-learned", action="store_true", help="bf16 backend without the learned pruning")
     ap.add_argument("--train-sample", type=int, default=200_000)
-    ap.add_argument("--train-epochs", type=int, default=30)
-    ap.add_argument("--train-quantile", type=float, default=0.05, help="pinball-loss quantile of the model")
+    ap.add_argument("--train-epochs", type=int, default=60)
+    ap.add_argument("--train-quantile", type=float, default=0.01, help="pinball-loss quantile of the model")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP32 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

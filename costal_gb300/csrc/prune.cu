@@ -257,10 +257,10 @@ __device__ __forceinline__ float block_ub_f32(const float* cq, float rq, const f
 }
 
 // Compare-exchange of list keys (descending) at a register distance S within a thread's run.
-template <int S>
-__device__ __forceinline__ void cx_regs(uint64_t (&v)[LIST_KPT], int base, int size) {
+template <int S, int KPT>
+__device__ __forceinline__ void cx_regs(uint64_t (&v)[KPT], int base, int size) {
 #pragma unroll
-    for (int j = 0; j < LIST_KPT; ++j) {
+    for (int j = 0; j < KPT; ++j) {
         const int p = j ^ S;
         if (p > j) {
             const bool desc = ((base + j) & size) == 0;
@@ -270,6 +270,79 @@ __device__ __forceinline__ void cx_regs(uint64_t (&v)[LIST_KPT], int base, int s
             v[p] = desc ? lo : hi;
         }
     }
+}
+
+// Bitonic sort (descending) of the CTA's LIST_T·KPT keys, KPT per thread at positions base..base+KPT−1:
+// compare-exchanges in registers, by warp shuffles, or through shared memory (xk) by distance.
+template <int KPT>
+__device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk, int base, int lane) {
+    constexpr int N = LIST_T * KPT;
+    for (int size = 2; size <= N; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= KPT * 32) {  // across warps
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < KPT; ++j) xk[base + j] = v[j];
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < KPT; ++j) {
+                    const int e = base + j;
+                    const uint64_t o = xk[e ^ stride];
+                    const bool keep_max = ((e & stride) == 0) == ((e & size) == 0);
+                    const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                    v[j] = keep_max ? hi : lo;
+                }
+            } else if (stride >= KPT) {  // within the warp
+                const int lstride = stride / KPT;
+#pragma unroll
+                for (int j = 0; j < KPT; ++j) {
+                    const int e = base + j;
+                    const uint64_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[j], lstride);
+                    const bool keep_max = ((lane & lstride) == 0) == ((e & size) == 0);
+                    const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                    v[j] = keep_max ? hi : lo;
+                }
+            } else if (stride == 8) {
+                if constexpr (KPT > 8) cx_regs<8>(v, base, size);
+            } else if (stride == 4) {
+                if constexpr (KPT > 4) cx_regs<4>(v, base, size);
+            } else if (stride == 2) {
+                cx_regs<2>(v, base, size);
+            } else {
+                cx_regs<1>(v, base, size);
+            }
+        }
+    }
+}
+
+// The sorted keys out: list position e holds block 8191 − (low 13 bits) and its bound.
+template <int KPT>
+__device__ __forceinline__ void write_keys(const uint64_t (&v)[KPT], int base, unsigned nk, uint32_t* out, float* out_ub) {
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        const unsigned e = (unsigned)(base + j);
+        if (e < nk) {
+            const uint32_t hk = (uint32_t)(v[j] >> 32);
+            out[e] = 8191u - ((uint32_t)v[j] & 8191u);
+            out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
+        }
+    }
+}
+
+// Compact the kept keys (non-zero) of every thread into xk[0 .. kept) in any order, zero-fill up to
+// LIST_T·KPT, and load KPT of them per thread.
+template <int KPT>
+__device__ __forceinline__ void compact_keys(const uint64_t (&all)[LIST_KPT], uint64_t (&v)[KPT], uint64_t* xk,
+                                             unsigned* slot, unsigned nk, int base) {
+    constexpr int N = LIST_T * KPT;
+    for (int e = threadIdx.x + (int)nk; e < N; e += LIST_T) xk[e] = 0ull;
+#pragma unroll
+    for (int j = 0; j < LIST_KPT; ++j)
+        if (all[j]) xk[atomicAdd(slot, 1u)] = all[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) v[j] = xk[base + j];
+    __syncthreads();  // every thread has its keys before the sort reuses xk
 }
 
 // One CTA per query block: the upper bound against every column block; the blocks kept (UB ≥ t_Q)
@@ -284,12 +357,13 @@ __global__ void __launch_bounds__(LIST_T, 2)
                   unsigned long long* __restrict__ skipped_total) {
     extern __shared__ uint64_t xk[];  // [LIST_N] exchange buffer
     __shared__ float cq[64];
-    __shared__ unsigned kept;
+    __shared__ unsigned kept, slot;
     __shared__ int skip_max_bits;
     const int Q = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
     if (tid < d) cq[tid] = (float)qcenter[(size_t)Q * d + tid];
     if (tid == 0) {
         kept = 0;
+        slot = 0;
         skip_max_bits = __float_as_int(-CUDART_INF_F);
     }
     __syncthreads();
@@ -344,53 +418,23 @@ __global__ void __launch_bounds__(LIST_T, 2)
         }
         atomicAdd(&kept, my_kept);
         atomicMax(&skip_max_bits, my_skip);
-        // the keys start interleaved over all LIST_N positions, so the sort always covers all of them
-        for (int size = 2; size <= LIST_N; size <<= 1) {
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                if (stride >= LIST_KPT * 32) {  // across warps
-                    __syncthreads();
-#pragma unroll
-                    for (int j = 0; j < LIST_KPT; ++j) xk[base + j] = v[j];
-                    __syncthreads();
-#pragma unroll
-                    for (int j = 0; j < LIST_KPT; ++j) {
-                        const int e = base + j;
-                        const uint64_t o = xk[e ^ stride];
-                        const bool keep_max = ((e & stride) == 0) == ((e & size) == 0);
-                        const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
-                        v[j] = keep_max ? hi : lo;
-                    }
-                } else if (stride >= LIST_KPT) {  // within the warp
-                    const int lstride = stride / LIST_KPT;
-#pragma unroll
-                    for (int j = 0; j < LIST_KPT; ++j) {
-                        const int e = base + j;
-                        const uint64_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[j], lstride);
-                        const bool keep_max = ((lane & lstride) == 0) == ((e & size) == 0);
-                        const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
-                        v[j] = keep_max ? hi : lo;
-                    }
-                } else if (stride == 8) {
-                    cx_regs<8>(v, base, size);
-                } else if (stride == 4) {
-                    cx_regs<4>(v, base, size);
-                } else if (stride == 2) {
-                    cx_regs<2>(v, base, size);
-                } else {
-                    cx_regs<1>(v, base, size);
-                }
-            }
-        }
         __syncthreads();  // kept is final
         const unsigned nk = kept;
-#pragma unroll
-        for (int j = 0; j < LIST_KPT; ++j) {
-            const unsigned e = (unsigned)(base + j);
-            if (e < nk) {
-                const uint32_t hk = (uint32_t)(v[j] >> 32);
-                out[e] = 8191u - ((uint32_t)v[j] & 8191u);
-                out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
-            }
+        // Short lists (a learned threshold skips most blocks) sort only their kept keys, compacted.
+        if (nk <= (unsigned)(LIST_T * 4)) {
+            uint64_t w[4];
+            compact_keys<4>(v, w, xk, &slot, nk, tid * 4);
+            block_sort_keys<4>(w, xk, tid * 4, lane);
+            write_keys<4>(w, tid * 4, nk, out, out_ub);
+        } else if (nk <= (unsigned)(LIST_T * 8)) {
+            uint64_t w[8];
+            compact_keys<8>(v, w, xk, &slot, nk, tid * 8);
+            block_sort_keys<8>(w, xk, tid * 8, lane);
+            write_keys<8>(w, tid * 8, nk, out, out_ub);
+        } else {
+            // the keys start interleaved over all LIST_N positions, so the sort covers all of them
+            block_sort_keys<LIST_KPT>(v, xk, base, lane);
+            write_keys<LIST_KPT>(v, base, nk, out, out_ub);
         }
     }
     __syncthreads();
