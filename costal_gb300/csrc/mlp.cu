@@ -39,9 +39,43 @@ __host__ __device__ inline Off offsets(int F) {
 }
 
 // ---- features ---------------------------------------------------------------------------------
-// One warp per row: 8 centroid cosines per lane, a branch-free warp bitonic sort of the 256 as
-// (cosine desc, centroid asc) keys, the first 64 kept. Centroids sit in shared memory with an odd
-// row stride, so the lanes' reads of 32 different centroids hit 32 different banks.
+// One warp per row: the row's (at most 64) coordinates loaded once, two per lane, and broadcast by
+// shuffles; 8 centroid cosines per lane; a branch-free warp bitonic sort of the 256 cosines
+// (descending; only the values are kept, so ties need no order), the first 64 kept. Centroids sit
+// in shared memory with an odd row stride, so the lanes' reads of 32 different centroids hit 32
+// different banks.
+
+// Bitonic sort of a warp-distributed array of floats (position p = s·32 + lane), descending.
+template <int SL>
+__device__ __forceinline__ void warp_sort_desc(float (&v)[SL], int lane) {
+    constexpr int N = 32 * SL;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+#pragma unroll
+                for (int s = 0; s < SL; ++s) {
+                    const int t = s ^ (stride >> 5);
+                    if (t > s) {
+                        const bool desc = ((s * 32 + lane) & size) == 0;
+                        const float hi = fmaxf(v[s], v[t]), lo = fminf(v[s], v[t]);
+                        v[s] = desc ? hi : lo;
+                        v[t] = desc ? lo : hi;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < SL; ++s) {
+                    const float o = __shfl_xor_sync(COSTAL_FULL_MASK, v[s], stride);
+                    const bool keep_max = ((lane & stride) == 0) == (((s * 32 + lane) & size) == 0);
+                    v[s] = keep_max ? fmaxf(v[s], o) : fminf(v[s], o);
+                }
+            }
+        }
+    }
+}
+
 __global__ void k_features(const float* __restrict__ xsT, int np, int d, const float* __restrict__ cent, int K,
                            const uint32_t* __restrict__ rows, int m, float* __restrict__ feat) {
     extern __shared__ float c_s[];  // [K][ds]
@@ -54,28 +88,28 @@ __global__ void k_features(const float* __restrict__ xsT, int np, int d, const f
     // grid-stride over rows, one warp per row: the centroids are loaded once per CTA
     for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
         const uint32_t r = rows ? rows[i] : (uint32_t)i;
+        const float x0 = lane < d ? xsT[(size_t)lane * np + r] : 0.0f;
+        const float x1 = lane + 32 < d ? xsT[(size_t)(lane + 32) * np + r] : 0.0f;
         float dot[8];
 #pragma unroll
         for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
         for (int t = 0; t < d; ++t) {
-            const float a = xsT[(size_t)t * np + r];
+            const float a = __shfl_sync(COSTAL_FULL_MASK, t < 32 ? x0 : x1, t & 31);
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 const int c = s * 32 + lane;
                 if (c < K) dot[s] = fmaf(a, c_s[c * ds + t], dot[s]);
             }
         }
-        uint64_t key[8];
 #pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            const int c = s * 32 + lane;
-            key[s] = c < K ? order_key(dot[s], (uint32_t)c) : PAD_KEY;
-        }
-        warp_sort_keys<8>(key, lane);
+        for (int s = 0; s < 8; ++s)
+            if (s * 32 + lane >= K) dot[s] = -CUDART_INF_F;
+        warp_sort_desc<8>(dot, lane);
         float* f = feat + (size_t)i * F;
-        for (int t = lane; t < d; t += 32) f[t] = xsT[(size_t)t * np + r];
-        f[d + lane] = key_score(key[0]);
-        f[d + 32 + lane] = key_score(key[1]);
+        if (lane < d) f[lane] = x0;
+        if (lane + 32 < d) f[lane + 32] = x1;
+        f[d + lane] = dot[0];
+        f[d + 32 + lane] = dot[1];
     }
 }
 
