@@ -45,26 +45,39 @@ __global__ void k_gather_rows(const float* __restrict__ xsT, int np, int d, cons
 }
 
 // Best centroid (largest dot with the unit centroid) of every row; rows are either a row-major
-// [m][d] array (rows_rm) or the columns of xsT. Centroids live in shared memory.
+// [m][d] array (rows_rm) or the columns of xsT. Centroids live in shared memory, rows padded to a
+// multiple of 4 with zeros, read 16 bytes at a time (every thread reads the same centroid: a
+// broadcast); the dot keeps the dimension order.
 __global__ void __launch_bounds__(KM_BLOCK) k_assign(const float* __restrict__ rows_rm, const float* __restrict__ xsT,
                                                      int np, int m, int d, const float* __restrict__ cent, int K,
                                                      uint32_t* __restrict__ assign) {
-    extern __shared__ float c_s[];  // [K][d]
-    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[e] = cent[e];
+    extern __shared__ float4 c_s4[];  // [K][dq/4]
+    float* c_s = reinterpret_cast<float*>(c_s4);
+    const int dq = (d + 3) & ~3, q4 = dq >> 2;
+    for (int e = threadIdx.x; e < K * dq; e += blockDim.x) {
+        const int c = e / dq, t = e - c * dq;
+        c_s[e] = t < d ? cent[c * d + t] : 0.0f;
+    }
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     float x[64];
 #pragma unroll
-    for (int t = 0; t < 64; ++t)
-        if (t < d) x[t] = rows_rm ? rows_rm[(size_t)i * d + t] : xsT[(size_t)t * np + i];
+    for (int t = 0; t < 64; ++t) x[t] = t < d ? (rows_rm ? rows_rm[(size_t)i * d + t] : xsT[(size_t)t * np + i]) : 0.0f;
     float best = -CUDART_INF_F;
     uint32_t arg = 0;
     for (int c = 0; c < K; ++c) {
         float s = 0.0f;
 #pragma unroll
-        for (int t = 0; t < 64; ++t)
-            if (t < d) s = fmaf(x[t], c_s[c * d + t], s);
+        for (int t4 = 0; t4 < 16; ++t4) {
+            if (t4 < q4) {
+                const float4 w = c_s4[c * q4 + t4];
+                s = fmaf(x[4 * t4], w.x, s);
+                s = fmaf(x[4 * t4 + 1], w.y, s);
+                s = fmaf(x[4 * t4 + 2], w.z, s);
+                s = fmaf(x[4 * t4 + 3], w.w, s);
+            }
+        }
         if (s > best) {
             best = s;
             arg = (uint32_t)c;
@@ -537,7 +550,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     S.sample_idx = reinterpret_cast<uint32_t*>(take((size_t)m * 4));
     P.scratch = S.sample_rows;
 
-    const size_t csm = (size_t)K * d * 4;
+    const size_t csm = (size_t)K * ((d + 3) & ~3) * 4;
     cudaError_t e = cudaFuncSetAttribute(k_assign, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm);
     if (e != cudaSuccess) return e;
     k_sample_idx<<<(m + 255) / 256, 256, 0, st>>>(S.sample_idx, m, n); note_launch();
