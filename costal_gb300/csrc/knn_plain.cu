@@ -15,6 +15,8 @@
 // an FP32 score ≤ τ, its exact score is within ε of it, and the certificate (or the regather)
 // makes the final ranking a function of the f64 rescoring alone (knn.rs:682-687).
 
+#include <algorithm>
+
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
@@ -198,8 +200,7 @@ constexpr int RS_ROWS = 8;
 constexpr int RS_MAXCAP = 128;
 
 template <int SLOTS>
-__global__ void __launch_bounds__(256)
-    k_rescore(const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
+__device__ __forceinline__ void rescore_group(int g, const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
               const uint32_t* __restrict__ cand_idx, const float* __restrict__ cand_score,
               const float* __restrict__ tau, const double* __restrict__ norms, const double* __restrict__ row_eps,
               const double* __restrict__ row_ub, unsigned* __restrict__ ub_fail, double eps, int certify, int select,
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(256)
     __shared__ int row_s[RS_ROWS], cnt_s[RS_ROWS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nrows = rlist ? (int)*rcount : n;
-    const int w0 = blockIdx.x * RS_ROWS;
+    const int w0 = g * RS_ROWS;
     if (w0 >= nrows) return;
     const int nr = min(RS_ROWS, nrows - w0);
     if (tid < RS_ROWS) row_s[tid] = tid < nr ? (rlist ? (int)rlist[w0 + tid] : w0 + tid) : 0;
@@ -355,6 +356,27 @@ __global__ void __launch_bounds__(256)
             out_cos[(size_t)i * k + p] = cs[s];
             if (out_w) out_w[(size_t)i * k + p] = tani_from_cos(ni, norms[id[s]], cs[s]);
         }
+    }
+}
+
+// Row groups of RS_ROWS, grid-stride: one group per CTA, or (deep rows) a few CTAs per SM walking
+// many groups, so that the rows each thread streams through stay in L1.
+template <int SLOTS>
+__global__ void __launch_bounds__(256)
+    k_rescore(const float* __restrict__ x, int n, int d, int k, int cap, int lstride,
+              const uint32_t* __restrict__ cand_idx, const float* __restrict__ cand_score,
+              const float* __restrict__ tau, const double* __restrict__ norms, const double* __restrict__ row_eps,
+              const double* __restrict__ row_ub, unsigned* __restrict__ ub_fail, double eps, int certify, int select,
+              const uint32_t* __restrict__ rlist,
+              const unsigned* __restrict__ rcount, uint32_t* __restrict__ out_idx, double* __restrict__ out_cos,
+              double* __restrict__ out_w, uint32_t* __restrict__ fb_rows, double* __restrict__ fb_minsim,
+              unsigned* __restrict__ fb_count, unsigned long long* __restrict__ max_err_bits) {
+    const int nrows = rlist ? (int)*rcount : n;
+    for (int g = blockIdx.x; g * RS_ROWS < nrows; g += gridDim.x) {
+        rescore_group<SLOTS>(g, x, n, d, k, cap, lstride, cand_idx, cand_score, tau, norms, row_eps, row_ub, ub_fail,
+                             eps, certify, select, rlist, rcount, out_idx, out_cos, out_w, fb_rows, fb_minsim, fb_count,
+                             max_err_bits);
+        __syncthreads();  // the group's shared arrays are free again
     }
 }
 
@@ -500,7 +522,16 @@ cudaError_t launch_rescore(const float* x, int n, int d, int k, int cap, int lst
                            uint32_t* out_idx, double* out_cos, double* out_w, uint32_t* fb_rows, double* fb_minsim,
                            unsigned* fb_count, unsigned long long* max_err_bits, cudaStream_t st) {
     const int slots = coarse_slots(cap);
-    const int blocks = (n + 7) / 8;
+    // deep rows: three CTAs per SM (their streamed rows fit L1); otherwise one CTA per group
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                       cudaSuccess)
+            sms = 148;
+    }
+    const int groups = (n + RS_ROWS - 1) / RS_ROWS;
+    const int blocks = d >= 256 ? std::min(groups, 3 * sms) : groups;
 #define COSTAL_RESCORE(S)                                                                                   \
     k_rescore<S><<<blocks, 256, 0, st>>>(x, n, d, k, cap, lstride, cand_idx, cand_score, tau, norms, row_eps, \
                                          row_ub, ub_fail, eps, certify, select, rlist, rcount, out_idx, out_cos, \
