@@ -160,7 +160,8 @@ def test_compact_operands_on_the_tensor_cores(ext, oracle, n, d, k, margin):
 @pytest.mark.parametrize("n,d,k,margin", [(700, 43, 10, None), (600, 300, 15, None), (500, 2000, 15, 15),
                                           (400, 130, 20, 40), (650, 41, 10, None), (640, 42, 12, 12)])
 def test_deep_rows_on_the_tensor_cores(ext, oracle, n, d, k, margin):
-    """Rows deeper than two K blocks run the tensor-core K loop (no locality order): same exact output."""
+    """Rows with 3d > 128 run the tensor-core K loop (no locality order); d = 41, 42 the resident
+    3d-wide form at its upper end: same exact output."""
     rng = np.random.default_rng(n + d)
     means = rng.normal(0, 2, size=(9, d))
     x = np.arcsinh((means[rng.integers(0, 9, n)] + rng.normal(0, 0.6, size=(n, d))) / 5.0).astype(np.float32)
@@ -339,3 +340,9 @@ def test_full_size_row_sample_parity(ext, oracle, name, rows, backend):
     assert (np.diff(idx, axis=1)[tie] > 0).all()
     s = np.sort(idx, axis=1)
     assert (np.diff(s, axis=1) > 0).all()
+    if backend == "bf16":
+        # every row, including those the tensor-core certificate sent to the FP32 re-run (merged over
+        # column segments) or a learned skip sent back: the same answer as the plain FP32 path
+        (fidx, fcos, _), _ = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="fp32")
+        np.testing.assert_array_equal(idx, fidx)
+        np.testing.assert_array_equal(cos, fcos)
