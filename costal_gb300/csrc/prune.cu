@@ -214,20 +214,32 @@ __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const
         center[(size_t)b * d + threadIdx.x] = c_s[threadIdx.x];
         if (center_f) center_f[(size_t)threadIdx.x * gridDim.x + b] = (float)c_s[threadIdx.x];  // [d][blocks]
     }
-    double worst = 0.0;
+    // The radius in f32 with a rigorous margin: the rows are unit vectors to within (d + 2)·2⁻²⁴, the
+    // f32 centre is the f64 one to 2⁻²⁴ per component, and the f32 dot and norm accumulate at most
+    // d·2⁻²⁴ of relative error each, so the f32 cosine is within (2d + 8)·2⁻²⁴ of the exact one; twice
+    // that is subtracted before acosf (itself within a few ulp, covered by 1e-6 rad), and every step
+    // rounds up. A zero row has cosine 0 with everything: angle π/2 covers it.
+    __shared__ float cf_s[64];
+    if (threadIdx.x < d) cf_s[threadIdx.x] = (float)c_s[threadIdx.x];
+    __syncthreads();
+    const float margin = (float)(2 * d + 8) * 0x1p-23f;
+    float worst = 0.0f;
     for (int w = r0 + threadIdx.x; w < r1; w += blockDim.x) {
         const uint32_t o = perm[w];
-        double dot = 0.0, nn = 0.0;
+        float dot = 0.0f, nn = 0.0f;
         for (int t = 0; t < d; ++t) {
-            const double v = (double)xsT[(size_t)t * np + o];
-            dot += v * c_s[t];
-            nn += v * v;
+            const float v = xsT[(size_t)t * np + o];
+            dot = fmaf(v, cf_s[t], dot);
+            nn = fmaf(v, v, nn);
         }
-        // zero rows have cosine 0 with everything: angle π/2 covers them
-        const double cs = nn > 0.0 ? dot / sqrt(nn) : 0.0;
-        worst = fmax(worst, acos(fmin(1.0, fmax(-1.0, cs))));
+        float ang = 1.57079637f;  // ≥ π/2
+        if (nn > 0.0f) {
+            const float cs = __fsub_rd(__fdiv_rd(dot, __fsqrt_ru(nn)), margin);
+            ang = __fadd_ru(acosf(fminf(1.0f, fmaxf(-1.0f, cs))), 1e-6f);
+        }
+        worst = fmaxf(worst, ang);
     }
-    red[threadIdx.x] = worst;
+    red[threadIdx.x] = (double)worst;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
