@@ -230,6 +230,49 @@ def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_kn
     return edges
 
 
+def _build_graph_csr(x, k, *, weight="tanimoto", margin=None, matmul=None, learned_prune=False):
+    """GB300 addition: the fused X -> kNN -> weights -> fuzzy union, handed back as the Leiden's CSR
+    (leiden.rs:52-101 `Csr::from_edges` of the edge list _build_graph returns), built on the device.
+
+    Returns (indptr uint64[n + 1], nbr uint32[nnz], weights float64[nnz]) for _leiden_csr."""
+    x = _arr(x, np.float32, 2, "x")
+    n, d = x.shape
+    wc = _weight_code(weight)
+    if matmul not in _BACKENDS:
+        raise ValueError(f'unknown matmul backend "{matmul}"')
+    k = int(k)
+    indptr = np.empty(n + 1, np.uint64)
+    nbr = np.empty(2 * n * k, np.uint32)
+    w = np.empty(2 * n * k, np.float64)
+    nnz = C.c_uint64(0)
+    st = L.KnnStats()
+    o = _opts("cosine", margin, None, None, _BACKENDS[matmul], True, True, learned_prune)
+    _call(L.lib().costal_build_graph_csr, _ptr(x), n, d, k, C.byref(o), wc, _ptr(indptr), _ptr(nbr), _ptr(w),
+          C.byref(nnz), C.byref(st))
+    nnz = nnz.value
+    return indptr, nbr[:nnz].copy(), w[:nnz].copy()
+
+
+def _leiden_csr(n, indptr, nbr, weights, *, resolution, beta=0.01, n_iterations=2, seed=0, n_threads=None):
+    """GB300 addition: _leiden on a graph given as the CSR _build_graph_csr returns, used in place.
+
+    Returns (membership int32, n_clusters, iterations, converged), the same as _leiden on the edge
+    list the CSR was built from."""
+    n = _u64(n, "n")
+    indptr = _arr(indptr, np.uint64, 1, "indptr")
+    nbr = _arr(nbr, np.uint32, 1, "nbr")
+    w = _arr(weights, np.float64, 1, "weights")
+    if len(indptr) != n + 1:
+        raise ValueError(f"indptr has {len(indptr)} entries for n={n}")
+    if int(indptr[-1]) != len(nbr) or len(nbr) != len(w):
+        raise ValueError(f"indptr ends at {int(indptr[-1])} but there are {len(nbr)} neighbours and {len(w)} weights")
+    memb = np.empty(n, np.uint32)
+    ncl, it, conv = C.c_uint64(), C.c_uint64(), C.c_int()
+    _call(L.lib().costal_leiden_csr, n, _ptr(indptr), _ptr(nbr), _ptr(w), 0, float(resolution), float(beta),
+          int(n_iterations), _u64(seed, "seed"), None, _ptr(memb), C.byref(ncl), C.byref(it), C.byref(conv), None)
+    return memb.view(np.int32), int(ncl.value), int(it.value), bool(conv.value)
+
+
 def _as_u32(a, name):
     """lib.rs:241-249: a non-negative int32 array viewed as u32."""
     a = _arr(a, np.int32, 1, name)

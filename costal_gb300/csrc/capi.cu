@@ -52,6 +52,7 @@ struct Misc {  // small device-side results read back at the end of a call
     unsigned long long timeout_flag;
     unsigned long long blocks_stopped;
     unsigned long long conv_mismatches;
+    unsigned nnz;
 };
 
 struct Context {
@@ -67,6 +68,7 @@ struct Context {
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
     DevBuf part_idx, part_score, part_tau, tfloor;
+    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w;
     MlpState mlp;
 };
 
@@ -600,6 +602,40 @@ int costal_build_graph(const float* x, uint64_t n, uint32_t d, uint32_t k, const
         if (idx) CK(cudaMemcpyAsync(idx, c.out_idx.p, nk * 4, cudaMemcpyDeviceToHost, s));
         if (cos) CK(cudaMemcpyAsync(cos, c.out_cos.p, nk * 8, cudaMemcpyDeviceToHost, s));
         if (norms) CK(cudaMemcpyAsync(norms, c.norms.p, n * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_build_graph_csr(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                           uint32_t weight, uint64_t* indptr, uint32_t* nbr, double* w, uint64_t* nnz,
+                           costal_knn_stats* stats, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        const uint64_t nk = n * k;
+        if (2 * nk > (uint64_t)INT32_MAX) throw Fail{COSTAL_EUNSUPPORTED, "2*n*k exceeds the int32 range of the GPU CSR"};
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = c.stream;
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.rows, nk * 4));
+        CK(ensure(c.cols, nk * 4));
+        CK(ensure(c.wout, nk * 8));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        uint64_t m = 0;
+        run_build(c, c.x.as<float>(), n, d, k, o, weight, c.rows.as<int32_t>(), c.cols.as<int32_t>(),
+                  c.wout.as<double>(), &m, stats, s);
+        CK(ensure(c.csr_ws, csr_scratch_bytes((int)n, (int)k)));
+        CK(ensure(c.csr_indptr, (n + 1) * 8));
+        CK(ensure(c.csr_src, 2 * nk * 4));
+        CK(ensure(c.csr_nbr, 2 * nk * 4));
+        CK(ensure(c.csr_w, 2 * nk * 8));
+        Misc* dm = c.misc.as<Misc>();
+        CK(launch_csr_from_union(c.rows.as<int32_t>(), c.cols.as<int32_t>(), c.wout.as<double>(), &dm->m, (int)n, (int)k,
+                                 c.csr_ws.p, c.csr_indptr.as<uint64_t>(), c.csr_src.as<int32_t>(),
+                                 c.csr_nbr.as<int32_t>(), c.csr_w.as<double>(), &dm->nnz, s));
+        *nnz = 2 * m;
+        CK(cudaMemcpyAsync(indptr, c.csr_indptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(nbr, c.csr_nbr.p, *nnz * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(w, c.csr_w.p, *nnz * 8, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     });
 }

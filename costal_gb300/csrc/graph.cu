@@ -446,9 +446,63 @@ __global__ void __launch_bounds__(512) k_sort_big(Scratch s, int32_t* __restrict
     }
 }
 
+// ---- the Leiden graph (CSR) from the fuzzy-union edge list ---------------------------------------
+// leiden.rs:52-101 `Csr::from_edges` walks the edges in order and appends j to row i and i to row j.
+// On the union's list (unique pairs i < j, ascending (i, j), no zero weights) that puts, in every
+// row v, first the lower neighbours u < v in ascending order (their edges come in the blocks of rows
+// u < v, in order of u), then the upper ones in ascending order (v's own block): every row ascending.
+// So the same bucket machinery builds it: both directions of each edge emitted (slot 2e: i → j,
+// slot 2e + 1: j → i), bucketed by source, each bucket sorted by destination (unique in a row).
+__global__ void k_csr_emit(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
+                           const double* __restrict__ w, const uint32_t* __restrict__ m_dev, uint64_t slots, Scratch s) {
+    const uint64_t m = *m_dev;
+    for (uint64_t e2 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e2 < slots;
+         e2 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t e = e2 >> 1;
+        uint32_t src = NONE;
+        if (e < m) {
+            const uint32_t i = (uint32_t)rows[e], j = (uint32_t)cols[e];
+            src = (e2 & 1) ? j : i;
+            s.hi[e2] = (e2 & 1) ? i : j;
+            s.v[e2] = w[e];
+            atomicAdd(&s.cnt[src], 1u);
+        }
+        s.lo[e2] = src;
+    }
+}
+
+__global__ void k_widen(const uint32_t* __restrict__ a, int len, uint64_t* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) out[i] = a[i];
+}
+
 }  // namespace fu
 
 size_t fuzzy_union_scratch_bytes(int n, int k) { return fu::scratch_bytes(n, k); }
+
+size_t csr_scratch_bytes(int n, int k) { return fu::scratch_bytes(n, 2 * k); }
+
+cudaError_t launch_csr_from_union(const int32_t* rows, const int32_t* cols, const double* w, const uint32_t* m_dev,
+                                  int n, int k, void* scratch, uint64_t* indptr, int32_t* src_out, int32_t* nbr,
+                                  double* w_out, uint32_t* nnz_dev, cudaStream_t st) {
+    using namespace fu;
+    const int k2 = 2 * k;  // two directed slots per union edge (at most n·k edges)
+    Scratch s = carve(scratch, n, k2);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.cnt, 0, (n + 1) * 4ull, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(s.cursor, 0, n * 4ull, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(s.nbig, 0, 4, st)) != cudaSuccess) return e;
+    k_csr_emit<<<2048, 256, 0, st>>>(rows, cols, w, m_dev, (uint64_t)n * k2, s); note_launch();
+    const int len = n + 1;
+    const int nb = (len + SCAN_B - 1) / SCAN_B;
+    k_scan_blocks<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum); note_launch();
+    k_scan_sums<<<1, SCAN_B, 0, st>>>(s.bsum, nb, nnz_dev); note_launch();
+    k_scan_add<<<nb, SCAN_B, 0, st>>>(s.cnt, len, s.bsum); note_launch();
+    k_scatter<<<2048, 256, 0, st>>>(n, k2, s); note_launch();
+    k_sort_small<<<(n + 7) / 8, 256, 0, st>>>(n, s, src_out, nbr, w_out); note_launch();
+    k_sort_big<<<256, 512, 0, st>>>(s, src_out, nbr, w_out); note_launch();
+    k_widen<<<(len + 255) / 256 < 4096 ? (len + 255) / 256 : 4096, 256, 0, st>>>(s.cnt, len, indptr); note_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t launch_fuzzy_union(const uint32_t* idx, const double* w, int n, int k, void* scratch, int32_t* rows,
                                int32_t* cols, double* w_out, uint32_t* m_dev, cudaStream_t st) {

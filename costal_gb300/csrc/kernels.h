@@ -56,6 +56,13 @@ cudaError_t launch_tanimoto_w(const uint32_t* idx, const double* cos, const doub
 cudaError_t launch_jaccard(const uint32_t* idx, int n, int k, uint32_t* sorted_scratch, double* out, cudaStream_t st);
 // Fuzzy union S + Sᵀ − S∘Sᵀ on the device. Scratch sizes in fuzzy_union_scratch_bytes.
 size_t fuzzy_union_scratch_bytes(int n, int k);
+// The Leiden CSR (leiden.rs:52-101 layout: indptr, both directions, rows in edge-list order, which
+// for the union's sorted list is ascending) from the union's edges rows/cols/w (m at m_dev on the
+// device): indptr[n + 1] (u64), nbr/w_out[2m], src_out[2m] the row of each entry; nnz at nnz_dev.
+size_t csr_scratch_bytes(int n, int k);
+cudaError_t launch_csr_from_union(const int32_t* rows, const int32_t* cols, const double* w, const uint32_t* m_dev,
+                                  int n, int k, void* scratch, uint64_t* indptr, int32_t* src_out, int32_t* nbr,
+                                  double* w_out, uint32_t* nnz_dev, cudaStream_t st);
 cudaError_t launch_fuzzy_union(const uint32_t* idx, const double* w, int n, int k, void* scratch, int32_t* rows,
                                int32_t* cols, double* w_out, uint32_t* m_dev, cudaStream_t st);
 

@@ -28,12 +28,28 @@
 
 namespace {
 
-struct Csr {  // leiden.rs:28-32
-    std::vector<size_t> indptr{0};
-    std::vector<uint32_t> nbr;
-    std::vector<double> w;
-    size_t n() const { return indptr.size() - 1; }
+// leiden.rs:28-32. The algorithm reads the graph through the three pointers, which point either into
+// the owned vectors (graphs built here) or into a caller's arrays (a CSR built on the GPU).
+struct Csr {
+    std::vector<size_t> indptr_s{0};
+    std::vector<uint32_t> nbr_s;
+    std::vector<double> w_s;
+    const size_t* indptr = indptr_s.data();
+    const uint32_t* nbr = nullptr;
+    const double* w = nullptr;
+    size_t nodes = 0;
+    size_t n() const { return nodes; }
+    void bind() {  // after the owned vectors change
+        indptr = indptr_s.data();
+        nbr = nbr_s.data();
+        w = w_s.data();
+        nodes = indptr_s.size() - 1;
+    }
+    Csr() = default;
+    Csr(const Csr&) = delete;
+    Csr& operator=(const Csr&) = delete;
 };
+static_assert(sizeof(size_t) == sizeof(uint64_t), "indptr is exchanged as u64");
 
 std::string fmt_f64(double x) {  // Rust's Display for the weights quoted in error messages
     if (std::isnan(x)) return "NaN";
@@ -50,7 +66,7 @@ bool csr_from_edges(size_t n, const uint32_t* rows, const uint32_t* cols, const 
         err = std::to_string(n) + " nodes exceed the u32 node index";
         return false;
     }
-    g.indptr.assign(n + 1, 0);
+    g.indptr_s.assign(n + 1, 0);
     for (size_t e = 0; e < m; ++e) {
         size_t i = rows[e], j = cols[e];
         double x = w[e];
@@ -69,26 +85,63 @@ bool csr_from_edges(size_t n, const uint32_t* rows, const uint32_t* cols, const 
             return false;
         }
         if (x > 0.0) {
-            g.indptr[i + 1] += 1;
-            g.indptr[j + 1] += 1;
+            g.indptr_s[i + 1] += 1;
+            g.indptr_s[j + 1] += 1;
         }
     }
-    for (size_t v = 0; v < n; ++v) g.indptr[v + 1] += g.indptr[v];
-    std::vector<size_t> fill(g.indptr.begin(), g.indptr.begin() + n);
-    g.nbr.assign(g.indptr[n], 0);
-    g.w.assign(g.indptr[n], 0.0);
+    for (size_t v = 0; v < n; ++v) g.indptr_s[v + 1] += g.indptr_s[v];
+    std::vector<size_t> fill(g.indptr_s.begin(), g.indptr_s.begin() + n);
+    g.nbr_s.assign(g.indptr_s[n], 0);
+    g.w_s.assign(g.indptr_s[n], 0.0);
     for (size_t e = 0; e < m; ++e) {
         size_t i = rows[e], j = cols[e];
         double x = w[e];
         if (x > 0.0) {
-            g.nbr[fill[i]] = (uint32_t)j;
-            g.w[fill[i]] = x;
+            g.nbr_s[fill[i]] = (uint32_t)j;
+            g.w_s[fill[i]] = x;
             fill[i] += 1;
-            g.nbr[fill[j]] = (uint32_t)i;
-            g.w[fill[j]] = x;
+            g.nbr_s[fill[j]] = (uint32_t)i;
+            g.w_s[fill[j]] = x;
             fill[j] += 1;
         }
     }
+    g.bind();
+    return true;
+}
+
+// A caller's CSR in the same layout (a graph built on the GPU), checked for what the algorithm
+// relies on — indptr from 0 and non-decreasing up to nnz, neighbours in range and not the row
+// itself, weights finite and positive — and used in place, without a copy.
+bool csr_view(size_t n, const uint64_t* indptr, const uint32_t* nbr, const double* w, Csr& g, std::string& err) {
+    if (n > 0xFFFFFFFFull) {
+        err = std::to_string(n) + " nodes exceed the u32 node index";
+        return false;
+    }
+    if (indptr[0] != 0) {
+        err = "indptr[0] must be 0";
+        return false;
+    }
+    for (size_t v = 0; v < n; ++v) {
+        if (indptr[v + 1] < indptr[v]) {
+            err = "indptr decreases at row " + std::to_string(v);
+            return false;
+        }
+        for (uint64_t e = indptr[v]; e < indptr[v + 1]; ++e) {
+            if (nbr[e] >= n || nbr[e] == v) {
+                err = "entry " + std::to_string(e) + " of row " + std::to_string(v) + " has neighbour " +
+                      std::to_string(nbr[e]) + " (n=" + std::to_string(n) + ")";
+                return false;
+            }
+            if (!(std::isfinite(w[e]) && w[e] > 0.0)) {
+                err = "entry " + std::to_string(e) + " has weight " + fmt_f64(w[e]) + "; CSR weights must be finite and positive";
+                return false;
+            }
+        }
+    }
+    g.indptr = reinterpret_cast<const size_t*>(indptr);
+    g.nbr = nbr;
+    g.w = w;
+    g.nodes = n;
     return true;
 }
 
@@ -548,9 +601,9 @@ void aggregate(const Csr& g, const double* nw, const std::vector<uint32_t>& labe
         out.nw[r] = s;
     }
     Csr& csr = out.g;
-    csr.indptr.assign(1, 0);
-    csr.nbr.clear();
-    csr.w.clear();
+    csr.indptr_s.assign(1, 0);
+    csr.nbr_s.clear();
+    csr.w_s.clear();
     reset(ws.acc, nl, 0.0);
     ws.touched.clear();
     for (size_t r = 0; r < nl; ++r) {
@@ -566,13 +619,14 @@ void aggregate(const Csr& g, const double* nw, const std::vector<uint32_t>& labe
         }
         std::sort(ws.touched.begin(), ws.touched.end());
         for (uint32_t q : ws.touched) {
-            csr.nbr.push_back(q);
-            csr.w.push_back(ws.acc[q]);
+            csr.nbr_s.push_back(q);
+            csr.w_s.push_back(ws.acc[q]);
             ws.acc[q] = 0.0;
         }
         ws.touched.clear();
-        csr.indptr.push_back(csr.nbr.size());
+        csr.indptr_s.push_back(csr.nbr_s.size());
     }
+    csr.bind();
 }
 
 // leiden.rs:648-751 — one iteration on the original graph; returns whether any node moved.
@@ -743,6 +797,26 @@ int costal_leiden(uint64_t n, const uint32_t* rows, const uint32_t* cols, const 
     Csr g;
     bool ok = from_coo ? csr_from_coo(n, rows, cols, weights, m, g, e) : csr_from_edges(n, rows, cols, weights, m, g, e);
     if (!ok) {
+        put_err(err, errlen, e);
+        return COSTAL_EINVAL;
+    }
+    Workspace ws;
+    if (!run(g, node_weights(g, objective), objective, resolution, beta, n_iterations, seed, initial, ws, membership,
+             n_clusters, iterations, converged, e)) {
+        put_err(err, errlen, e);
+        return COSTAL_EINVAL;
+    }
+    if (quality_out) *quality_out = quality(g, membership, objective, resolution);
+    return COSTAL_OK;
+}
+
+int costal_leiden_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, const double* weights, int objective,
+                      double resolution, double beta, int32_t n_iterations, uint64_t seed, const uint32_t* initial,
+                      uint32_t* membership, uint64_t* n_clusters, uint64_t* iterations, int* converged,
+                      double* quality_out, char* err, size_t errlen) {
+    std::string e;
+    Csr g;
+    if (!csr_view(n, indptr, nbr, weights, g, e)) {
         put_err(err, errlen, e);
         return COSTAL_EINVAL;
     }

@@ -112,6 +112,12 @@ int costal_fuzzy_union(uint64_t n, uint32_t k, const int32_t* idx, const double*
 int costal_build_graph(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
                        uint32_t weight, int32_t* rows, int32_t* cols, double* w, uint64_t* m, uint32_t* idx,
                        double* cos, double* norms, costal_knn_stats* stats, char* err, size_t errlen);
+/* GB300 addition: the same pipeline, with the graph handed back in the CSR layout the Leiden uses
+ * (leiden.rs:52-101 `Csr::from_edges` of the edge list: rows ascending; see costal_leiden_csr), built
+ * on the device. indptr holds n+1 u64; nbr/w hold up to 2*n*k entries; *nnz = 2 * edges. */
+int costal_build_graph_csr(const float* x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                           uint32_t weight, uint64_t* indptr, uint32_t* nbr, double* w, uint64_t* nnz,
+                           costal_knn_stats* stats, char* err, size_t errlen);
 /* The same from device-resident X, with device outputs (capacity n*k edges); *m is written on the host. */
 int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
                               uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m,
@@ -174,6 +180,14 @@ int costal_leiden(uint64_t n, const uint32_t* rows, const uint32_t* cols, const 
                   int objective, int from_coo, double resolution, double beta, int32_t n_iterations,
                   uint64_t seed, const uint32_t* initial, uint32_t* membership, uint64_t* n_clusters,
                   uint64_t* iterations, int* converged, double* quality, char* err, size_t errlen);
+/* GB300 addition (the first "next" item of the path): the same Leiden on a graph given directly in
+   the CSR layout of leiden.rs:52-101 `Csr::from_edges` (indptr n+1 u64 from 0; for every row its
+   neighbours and weights, both directions of every edge), as costal_build_graph_csr produces it;
+   used in place, without building a CSR from an edge list. Weights must be finite and positive. */
+int costal_leiden_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, const double* weights, int objective,
+                      double resolution, double beta, int32_t n_iterations, uint64_t seed, const uint32_t* initial,
+                      uint32_t* membership, uint64_t* n_clusters, uint64_t* iterations, int* converged,
+                      double* quality, char* err, size_t errlen);
 /* lib.rs:311-350 `_leiden_many`: out is (n_resolutions * n_seeds) x n, resolutions outer. */
 int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
                        const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,

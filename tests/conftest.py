@@ -109,6 +109,25 @@ def planted(n_blocks=12, size=40, p_in=0.15, n_cross=500, seed=0):
     return n, rows, cols, w
 
 
+def csr_from_edges(n, rows, cols, w):
+    """leiden.rs:52-101 `Csr::from_edges`, restated: walk the edges in order, append j to row i and i
+    to row j (zero weights dropped). Returns (indptr uint64, nbr uint32, weights float64)."""
+    rows = np.asarray(rows).astype(np.int64)
+    cols = np.asarray(cols).astype(np.int64)
+    w = np.asarray(w, dtype=np.float64)
+    keep = w > 0
+    rows, cols, w = rows[keep], cols[keep], w[keep]
+    # entry 2e is edge e seen from its first endpoint, 2e + 1 from its second: a stable sort by row
+    # keeps each row's entries in edge order
+    src = np.stack([rows, cols], 1).ravel()
+    dst = np.stack([cols, rows], 1).ravel()
+    ww = np.repeat(w, 2)
+    order = np.argsort(src, kind="stable")
+    indptr = np.zeros(n + 1, np.uint64)
+    np.cumsum(np.bincount(src, minlength=n), out=indptr[1:])
+    return indptr, dst[order].astype(np.uint32), ww[order]
+
+
 def pipeline_input():
     """The GOLDEN_PIPELINE input of the reference's tests/test_leiden_native.py:132-135."""
     rng = np.random.default_rng(7)

@@ -9,7 +9,7 @@ row samples (the oracle answers a sample of query rows against all n columns).
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_PIPELINE, Lcg, clustered, digest, lcg_clustered, pipeline_input
+from conftest import GOLDEN_PIPELINE, Lcg, clustered, csr_from_edges, digest, lcg_clustered, pipeline_input
 
 pytestmark = pytest.mark.gpu
 
@@ -249,6 +249,36 @@ def test_golden_pipeline_digest_on_gpu(ext):
     rows2, cols2, ew2 = ext._build_graph(x, 10)
     m2 = ext._leiden(len(x), rows2, cols2, ew2, resolution=0.8, n_iterations=2, seed=3)[0]
     assert digest(m2.astype(np.int64)) == GOLDEN_PIPELINE
+
+
+def test_graph_csr_built_on_the_device(ext):
+    # The Leiden's CSR (leiden.rs:52-101 of the union's edge list) built on the GPU: the same arrays
+    # as the host construction, and the golden labels from the host Leiden run on it in place.
+    x = pipeline_input()
+    indptr, nbr, w = ext._build_graph_csr(x, 10)
+    rows, cols, ew = ext._build_graph(x, 10)
+    want = csr_from_edges(len(x), rows, cols, ew)
+    for got, exp in zip((indptr, nbr, w), want):
+        np.testing.assert_array_equal(got, exp)
+    m = ext._leiden_csr(len(x), indptr, nbr, w, resolution=0.8, n_iterations=2, seed=3)[0]
+    assert digest(m.astype(np.int64)) == GOLDEN_PIPELINE
+    # hubs: two centres, each the nearest neighbour of the ~6,000 rows around it (rows of the CSR
+    # longer than one warp's bucket sort and than one shared-memory run of the large-bucket sort)
+    rng = np.random.default_rng(8)
+    d = 64
+    u = rng.normal(size=(12000, d))
+    side = np.arange(12000) % 2
+    u[np.arange(12000), side] = 0.0  # spokes orthogonal to their centre e_0 or e_1
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    pts = np.eye(d)[side] + 0.3 * u
+    x = np.ascontiguousarray(np.vstack([np.eye(d)[:2], pts]), dtype=np.float32)
+    for matmul in ("gemm", "bf16"):
+        indptr, nbr, w = ext._build_graph_csr(x, 15, matmul=matmul)
+        rows, cols, ew = ext._build_graph(x, 15, matmul=matmul)
+        want = csr_from_edges(len(x), rows, cols, ew)
+        assert np.diff(want[0].astype(np.int64)).max() > 4096
+        for got, exp in zip((indptr, nbr, w), want):
+            np.testing.assert_array_equal(got, exp)
 
 
 def test_golden_fixtures(ext):

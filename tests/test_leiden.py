@@ -4,7 +4,7 @@ no GPU needed. Restates the reference's tests/test_leiden_native.py and leiden.r
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_GRAPH, digest, planted
+from conftest import GOLDEN_GRAPH, csr_from_edges, digest, planted
 
 
 def test_golden_graph_digest(ext):
@@ -94,3 +94,34 @@ def test_cpm_quality_matches_its_definition(ext):
     sizes = np.bincount(labels)
     internal = sum(x for a, b, x in edges if labels[a] == labels[b])
     assert q == pytest.approx(2 * internal - 0.1 * float((sizes * (sizes - 1)).sum()), abs=1e-12)
+
+
+def test_csr_entry_matches_the_edge_list_and_checks_its_input(ext):
+    # the same Leiden on the graph given as its CSR (the GPU-built layout), used in place
+    n, rows, cols, w = planted(n_blocks=20, size=50, p_in=0.1, n_cross=2000, seed=11)
+    indptr, nbr, cw = csr_from_edges(n, rows, cols, w)
+    m = ext._leiden_csr(n, indptr, nbr, cw, resolution=1.3, seed=12345)[0]
+    assert digest(m) == GOLDEN_GRAPH
+    for seed in (0, 7):
+        a = ext._leiden(n, rows, cols, w, resolution=0.9, seed=seed)
+        b = ext._leiden_csr(n, indptr, nbr, cw, resolution=0.9, seed=seed)
+        assert np.array_equal(a[0], b[0]) and a[1:] == b[1:]
+    bad = indptr.copy()
+    bad[0] = 1
+    with pytest.raises(ValueError, match="indptr"):
+        ext._leiden_csr(n, bad, nbr, cw, resolution=1.0)
+    bad = indptr.copy()
+    bad[5], bad[6] = bad[6], bad[5]
+    with pytest.raises(ValueError, match="decreases"):
+        ext._leiden_csr(n, bad, nbr, cw, resolution=1.0)
+    for v in (np.uint32(n), np.uint32(0)):  # out of range; a self-loop on row 0
+        nb = nbr.copy()
+        nb[0] = v
+        with pytest.raises(ValueError, match="neighbour"):
+            ext._leiden_csr(n, indptr, nb, cw, resolution=1.0)
+    ww = cw.copy()
+    ww[3] = 0.0
+    with pytest.raises(ValueError, match="positive"):
+        ext._leiden_csr(n, indptr, nbr, ww, resolution=1.0)
+    with pytest.raises(ValueError, match="entries"):
+        ext._leiden_csr(n + 1, indptr, nbr, cw, resolution=1.0)

@@ -7,7 +7,7 @@ checker of every GPU parity test, so it must first reproduce what the reference 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_PIPELINE, Lcg, clustered, digest, lcg_clustered, pipeline_input
+from conftest import GOLDEN_PIPELINE, Lcg, clustered, csr_from_edges, digest, lcg_clustered, pipeline_input
 
 
 def same(a, b):
@@ -218,6 +218,21 @@ def test_golden_pipeline_digest(oracle, ext):
     w = oracle.reweight(idx, cos, norms, "tanimoto")
     r, c, v = oracle.fuzzy_union(idx, w)
     m = ext._leiden(len(x), r.view(np.int32), c.view(np.int32), v, resolution=0.8, n_iterations=2, seed=3)[0]
+    assert digest(m.astype(np.int64)) == GOLDEN_PIPELINE
+
+
+def test_golden_pipeline_on_the_csr_layout(oracle, ext):
+    # The Leiden's CSR of the union's edge list (leiden.rs:52-101): every row comes out ascending,
+    # the property the GPU's sorted buckets reproduce, and the host Leiden run on that CSR in place
+    # gives the golden labels.
+    x = pipeline_input()
+    (idx, cos, norms), _ = oracle.knn_exact(x, 10)
+    w = oracle.reweight(idx, cos, norms, "tanimoto")
+    r, c, v = oracle.fuzzy_union(idx, w)
+    indptr, nbr, cw = csr_from_edges(len(x), r, c, v)
+    for i in range(len(x)):
+        assert (np.diff(nbr[indptr[i]:indptr[i + 1]].astype(np.int64)) > 0).all()
+    m = ext._leiden_csr(len(x), indptr, nbr, cw, resolution=0.8, n_iterations=2, seed=3)[0]
     assert digest(m.astype(np.int64)) == GOLDEN_PIPELINE
 
 
