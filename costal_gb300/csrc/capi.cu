@@ -68,7 +68,7 @@ struct Context {
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
     DevBuf part_idx, part_score, part_tau, tfloor;
-    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w;
+    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm;
     MlpState mlp;
 };
 
@@ -204,13 +204,37 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaEventRecord(c.ev[5], s));
     const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
     bool used_tc = false;
-    if (tanimoto) {
-        // Tanimoto selection (knn.rs:197-284): the exact f64 scan of every candidate on the GPU
-        // (knn.rs:884-924's brute force), which is exact by construction.
+    if (tanimoto && coarse_fp32_smem(dp, cap) > 227 * 1024) {
+        // (a cap too large for the coarse kernel's shared memory) the exact f64 scan of every
+        // candidate on the GPU (knn.rs:884-924's brute force), exact by construction
         CK(cudaEventRecord(c.ev[2], s));
         CK(cudaEventRecord(c.ev[3], s));
         CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, nullptr, nullptr, nullptr, 1, 1,
                          std::min(n, 8 * c.sm_count), d_idx, d_cos, d_w, s));
+    } else if (tanimoto) {
+        // Tanimoto selection (knn.rs:197-284): the FP32 pass over all columns with the coarse
+        // Tanimoto score, the f64 rescoring of the cap candidates by T with the certificate
+        // s_k > τ + 2(d+12)·2⁻²³, and the regather (filtered by the coarse T) for rows that fail it.
+        CK(ensure(c.cand_idx, (size_t)n * cap * 4));
+        CK(ensure(c.cand_score, (size_t)n * cap * 4));
+        CK(ensure(c.tau, (size_t)n * 4));
+        CK(ensure(c.tnorm, (size_t)n * 8));
+        const double eps_t = 2.0 * ((double)d + 12.0) * F32_EPS;
+        CK(launch_coarse_fp32_tanimoto(c.xsT.as<float>(), n, np, dp, cap, d_norms, c.tnorm.as<float2>(),
+                                       c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
+        CK(cudaEventRecord(c.ev[2], s));
+        CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                          c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps_t, cap < n - 1, 1, nullptr,
+                          nullptr, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
+                          &dm->fb_count, &dm->max_err_bits, s));
+        CK(cudaEventRecord(c.ev[3], s));
+        if (cap < n - 1) {
+            if (gather_smem(k, d, dp) > 227 * 1024)
+                throw Fail{COSTAL_EUNSUPPORTED, "k too large for the GPU regather kernel"};
+            CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, c.fb_rows.as<uint32_t>(),
+                             c.fb_minsim.as<double>(), &dm->fb_count, 0, 1, std::min(n, 4 * c.sm_count), d_idx,
+                             d_cos, d_w, s));
+        }
     } else {
         CK(ensure(c.cand_idx, (size_t)n * cap * 4));
         CK(ensure(c.cand_score, (size_t)n * cap * 4));

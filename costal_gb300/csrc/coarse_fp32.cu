@@ -165,12 +165,29 @@ __device__ __forceinline__ void select_tile(const float (&acc)[8][8], int c0, in
     }
 }
 
-template <int SLOTS, int DPC>
+// The tile's 8 × 8 cosines → Tanimoto scores (rows qi_of(i), columns c0 + cj_of(j)).
+__device__ __forceinline__ void tani_tile(float (&acc)[8][8], const float2* __restrict__ tnorm, int c0, int n, int tx,
+                                          int ty, const int* rows8) {
+    float2 cn[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int col = c0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+        cn[j] = col < n ? tnorm[col] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float2 qn = rows8[i] >= 0 ? tnorm[rows8[i]] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = tani_coarse_f32(acc[i][j], qn, cn[j]);
+    }
+}
+
+template <int SLOTS, int DPC, bool TANI>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp_rt, int cap, int lstride,
                   const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
-                  const float* __restrict__ tfloor, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
-                  float* __restrict__ tau_out) {
+                  const float* __restrict__ tfloor, const float2* __restrict__ tnorm, uint32_t* __restrict__ cand_idx,
+                  float* __restrict__ cand_score, float* __restrict__ tau_out) {
     constexpr int LCAP = 32 * SLOTS;
     const int dp = DPC ? DPC : dp_rt;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -283,13 +300,26 @@ __global__ void __launch_bounds__(NT, 1)
                 for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
         }
 #endif
-
+        if constexpr (TANI) {
+            int rows8[8];  // this thread's 8 query rows (their norms enter the Tanimoto scores)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = row_of(i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+                rows8[i] = r < n ? r : -1;
+            }
+            tani_tile(acc, tnorm, c0, n, tx, ty, rows8);
+        }
         select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
                            row_of,
                            [&](int qi, int cl) {
                                float sv = 0.0f;
 #pragma unroll(DPC ? DPC : 4)
                                for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
+                               if constexpr (TANI) {
+                                   const int q = row_of(qi), col = c0 + cl;
+                                   sv = tani_coarse_f32(sv, q >= 0 ? tnorm[q] : make_float2(0.0f, 0.0f),
+                                                    col < n ? tnorm[col] : make_float2(0.0f, 0.0f));
+                               }
                                return sv;
                            });
     }
@@ -302,12 +332,12 @@ __global__ void __launch_bounds__(NT, 1)
 // of the transposed copy (query chunk and column chunk per stage), and the 8 × 8 register tile
 // accumulates across the chunks of a tile in dimension order, so every score is the same FMA chain
 // as in k_coarse_fp32. A query whose buffer overflows is recomputed from global memory.
-template <int SLOTS, int KC>
+template <int SLOTS, int KC, bool TANI>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32_kc(const float* __restrict__ xsT, int n, int np, int dp, int cap, int lstride,
                      const uint32_t* __restrict__ qlist, const unsigned* __restrict__ qcount, int part_stride,
-                     const float* __restrict__ tfloor, uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score,
-                     float* __restrict__ tau_out) {
+                     const float* __restrict__ tfloor, const float2* __restrict__ tnorm, uint32_t* __restrict__ cand_idx,
+                     float* __restrict__ cand_score, float* __restrict__ tau_out) {
     constexpr int LCAP = 32 * SLOTS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* S_s = reinterpret_cast<float*>(smem_raw);            // [STAGES][KC][BM + BN]
@@ -410,6 +440,15 @@ __global__ void __launch_bounds__(NT, 1)
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
+        if constexpr (TANI) {
+            int rows8[8];  // this thread's 8 query rows (their norms enter the Tanimoto scores)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = row_of(i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+                rows8[i] = r < n ? r : -1;
+            }
+            tani_tile(acc, tnorm, c0, n, tx, ty, rows8);
+        }
         select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
                            row_of,
                            [&](int qi, int cl) {
@@ -419,6 +458,11 @@ __global__ void __launch_bounds__(NT, 1)
                                if (q >= 0)
                                    for (int t = 0; t < dp; ++t)
                                        sv = fmaf(xsT[(size_t)t * np + q], xsT[(size_t)t * np + c0 + cl], sv);
+                               if constexpr (TANI) {
+                                   const int col = c0 + cl;
+                                   sv = tani_coarse_f32(sv, q >= 0 ? tnorm[q] : make_float2(0.0f, 0.0f),
+                                                    col < n ? tnorm[col] : make_float2(0.0f, 0.0f));
+                               }
                                return sv;
                            });
     }
@@ -436,14 +480,15 @@ size_t coarse_smem_bytes_kc(int slots) {
 
 template <int S>
 cudaError_t launch_kc(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                      const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
-                      float* cand_score, float* tau, cudaStream_t st) {
+                      const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, const float2* tnorm,
+                      uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
     constexpr int KC = kc_for(S);
     const size_t smem = coarse_smem_bytes_kc(S);
-    cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32_kc<S, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = tnorm ? k_coarse_fp32_kc<S, KC, true> : k_coarse_fp32_kc<S, KC, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_coarse_fp32_kc<S, KC><<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
-        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, cand_idx, cand_score, tau);
+    kern<<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
+        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, tnorm, cand_idx, cand_score, tau);
     note_launch();
     return cudaGetLastError();
 }
@@ -456,39 +501,40 @@ size_t coarse_smem_bytes(int dp, int slots) {
 
 template <int S, int D>
 cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
-                       float* cand_score, float* tau, cudaStream_t st) {
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor,
+                       const float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
     const size_t smem = coarse_smem_bytes(dp, S);
-    cudaError_t e = cudaFuncSetAttribute(k_coarse_fp32<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = tnorm ? k_coarse_fp32<S, D, true> : k_coarse_fp32<S, D, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_coarse_fp32<S, D><<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
-        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, cand_idx, cand_score, tau);
+    kern<<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
+        xsT, n, np, dp, cap, lstride, qlist, qcount, part_stride, tfloor, tnorm, cand_idx, cand_score, tau);
     note_launch();
     return cudaGetLastError();
 }
 
 template <int S>
 cudaError_t dispatch_d(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
-                       float* cand_score, float* tau, cudaStream_t st) {
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor,
+                       const float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
 #define COSTAL_D(D)                                                                                            \
     case D:                                                                                                    \
         return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, \
-                                cand_idx, cand_score, tau, st);
+                                tnorm, cand_idx, cand_score, tau, st);
     switch (dp) {
         COSTAL_D(8) COSTAL_D(16) COSTAL_D(24) COSTAL_D(32) COSTAL_D(40) COSTAL_D(48) COSTAL_D(56) COSTAL_D(64)
         default:
             return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride,
-                                    tfloor, cand_idx, cand_score, tau, st);
+                                    tfloor, tnorm, cand_idx, cand_score, tau, st);
     }
 #undef COSTAL_D
 }
 
 cudaError_t launch_any(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
-                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor, uint32_t* cand_idx,
-                       float* cand_score, float* tau, cudaStream_t st) {
-#define COSTAL_ARGS xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, cand_idx, cand_score, \
-    tau, st
+                       const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor,
+                       const float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
+#define COSTAL_ARGS xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, tnorm, cand_idx, \
+    cand_score, tau, st
     if (dp > 64) {  // deep rows: the chunked kernel
         switch (coarse_slots(cap)) {
             case 1: return launch_kc<1>(COSTAL_ARGS);
@@ -563,8 +609,24 @@ int coarse_dpad(int d) { return d <= 64 ? ((d < 1 ? 1 : d) + 7) / 8 * 8 : (d + 3
 cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap, int lstride, const uint32_t* qlist,
                                const unsigned* qcount, uint32_t* cand_idx, float* cand_score, float* tau,
                                cudaStream_t st) {
-    return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, 0, 0, nullptr, cand_idx, cand_score, tau,
-                             st);
+    return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, 0, 0, nullptr, nullptr, cand_idx, cand_score,
+                             tau, st);
+}
+
+// The rows' f32 norm and squared norm from the f64 norms (knn.rs:207-212 rounds ‖x‖² to f32).
+__global__ void k_tani_norms(const double* __restrict__ norms, int n, float2* __restrict__ tnorm) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = norms[i];
+        tnorm[i] = make_float2((float)a, (float)(a * a));
+    }
+}
+
+cudaError_t launch_coarse_fp32_tanimoto(const float* xsT, int n, int np, int dp, int cap, const double* norms,
+                                        float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau,
+                                        cudaStream_t st) {
+    k_tani_norms<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, st>>>(norms, n, tnorm); note_launch();
+    return plain::launch_any(xsT, n, np, dp, cap, cap, nullptr, nullptr, 1, 0, 0, nullptr, tnorm, cand_idx, cand_score,
+                             tau, st);
 }
 
 int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
@@ -583,9 +645,9 @@ cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, in
                                      const float* tfloor, uint32_t* part_idx, float* part_score, float* part_tau,
                                      uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
     if (segs <= 1)
-        return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, count, 0, tfloor, cand_idx, cand_score,
-                                 tau, st);
-    cudaError_t e = plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, count, count, tfloor,
+        return plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, 1, count, 0, tfloor, nullptr, cand_idx,
+                                 cand_score, tau, st);
+    cudaError_t e = plain::launch_any(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, count, count, tfloor, nullptr,
                                       part_idx, part_score, part_tau, st);
     if (e != cudaSuccess) return e;
     plain::k_merge_parts<<<(count + 7) / 8, 256, 0, st>>>(qlist, count, segs, cap, part_idx, part_score, tfloor,

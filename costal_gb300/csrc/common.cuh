@@ -62,6 +62,18 @@ __device__ __forceinline__ double tani_from_cos(double a, double b, double c) {
     return __ddiv_rn(d, den);
 }
 
+// Tanimoto selection (knn.rs:197-284): the coarse score of a pair from an f32 cosine ĉ of the
+// normalised rows and the rows' f32 norms (x) and squared norms (y): T = dot / (A + B − dot) with
+// dot = a·b·ĉ, 0 when dot is 0 or the denominator is not positive (knn.rs:254-262). Within
+// 2(d+12)·2⁻²³ of the exact T: ∂T/∂dot ≤ 4/(A+B) and a·b ≤ (A+B)/2 turn ĉ's (d+4)·2⁻²³ into
+// 2(d+4)·2⁻²³, and the f32 norms and the four roundings add at most 8·2⁻²³ more (the argument of
+// knn.rs:270-274).
+__device__ __forceinline__ float tani_coarse_f32(float c, float2 qn, float2 cn) {
+    const float dn = qn.x * cn.x * c;
+    const float den = qn.y + cn.y - dn;
+    return (dn == 0.0f || den <= 0.0f) ? 0.0f : __fdiv_rn(dn, den);
+}
+
 // Rust's f64::total_cmp as a signed integer key (knn.rs:589-591 sorts with it).
 __device__ __forceinline__ long long total_key(double v) {
     long long b = __double_as_longlong(v);

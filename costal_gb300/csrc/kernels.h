@@ -27,6 +27,12 @@ cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, in
                                      const uint32_t* qlist, const unsigned* qcount, int count, int segs,
                                      const float* tfloor, uint32_t* part_idx, float* part_score, float* part_tau,
                                      uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st);
+// Tanimoto selection (knn.rs:197-284): the same FP32 pass over all columns with the coarse score
+// T = a·b·ĉ / (A + B − a·b·ĉ) from the normalised tile and the rows' norms (tnorm: n entries of
+// scratch, filled here); within 2(d+12)·2⁻²³ of the exact T.
+cudaError_t launch_coarse_fp32_tanimoto(const float* xsT, int n, int np, int dp, int cap, const double* norms,
+                                        float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau,
+                                        cudaStream_t st);
 // The floor of rows re-run after the tensor-core pass (rows[0..*count), cand_* and tau of that pass).
 cudaError_t launch_rerun_floor(const uint32_t* rows, const unsigned* count, int nmax, int cap, const float* tau,
                                const float* cand_score, const double* row_eps, double eps, float* tfloor,

@@ -448,6 +448,11 @@ __global__ void __launch_bounds__(GT)
                 if (!all_rows) {
                     float s = 0.0f;
                     for (int t = 0; t < dp; ++t) s = fmaf(q_s[t], xsT[(size_t)t * np + c], s);
+                    if (select != 0) {  // minsim is a Tanimoto score: compare the coarse T
+                        const double nj = norms[c];
+                        s = tani_coarse_f32(s, make_float2((float)ni, (float)(ni * ni)),
+                                            make_float2((float)nj, (float)(nj * nj)));
+                    }
                     take = (double)s >= ms;
                 }
                 if (take) {

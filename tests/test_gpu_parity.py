@@ -181,6 +181,30 @@ def test_tanimoto_selection_matches_bruteforce(ext, oracle):
     assert not np.array_equal(got[0], ext._knn_exact(x, 10)[0][0])
 
 
+@pytest.mark.parametrize("n,d,k,margin", [(2000, 16, 10, None), (1200, 40, 15, 5), (900, 65, 8, None),
+                                          (600, 300, 12, 12), (700, 7, 30, 0)])
+def test_tanimoto_selection_shapes(ext, oracle, n, d, k, margin):
+    # knn.rs:197-284 on the GPU: the FP32 pass with the coarse Tanimoto score (both the resident and
+    # the chunked kernel), rescoring by T and its certificate; rows of very different norms
+    rng = np.random.default_rng(n + 7 * d)
+    means = rng.normal(0, 2, size=(6, d))
+    x = (means[rng.integers(0, 6, n)] + rng.normal(0, 0.7, size=(n, d))) * rng.uniform(0.2, 5.0, size=(n, 1))
+    x = np.ascontiguousarray(np.abs(x), dtype=np.float32)
+    got, st = ext._knn_exact(x, k, select="tanimoto", margin=margin)
+    same(as_oracle(got), oracle.knn_bruteforce(x, k, select="tanimoto"))
+
+
+def test_tanimoto_selection_ties_take_the_regather(ext, oracle):
+    # integer rows repeat exactly: equal Tanimoto scores everywhere, certificate failures, and the
+    # regather filtered by the coarse Tanimoto score
+    rng = np.random.default_rng(15)
+    x = np.floor(rng.uniform(0, 3, size=(600, 5))).astype(np.float32)
+    x[[3, 300]] = 0.0
+    got, st = ext._knn_exact(x, 12, select="tanimoto")
+    same(as_oracle(got), oracle.knn_bruteforce(x, 12, select="tanimoto"))
+    assert st["fallback_rows"] > 0
+
+
 @pytest.mark.parametrize("weight", ["tanimoto", "cosine", "jaccard"])
 def test_reweight_bitwise(ext, oracle, weight):
     x = clustered(2000, 12, 8)
