@@ -504,7 +504,10 @@ cudaError_t launch_one(const float* xsT, int n, int np, int dp, int cap, int lst
                        const unsigned* qcount, int segs, int grid_rows, int part_stride, const float* tfloor,
                        const float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau, cudaStream_t st) {
     const size_t smem = coarse_smem_bytes(dp, S);
-    auto kern = tnorm ? k_coarse_fp32<S, D, true> : k_coarse_fp32<S, D, false>;
+    // (the Tanimoto variant is built only for a run-time depth: dispatch_d sends it there)
+    auto kern = k_coarse_fp32<S, D, false>;
+    if constexpr (D == 0)
+        if (tnorm) kern = k_coarse_fp32<S, 0, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<dim3(grid_rows ? (grid_rows + BM - 1) / BM : np / BM, segs), NT, smem, st>>>(
@@ -520,6 +523,9 @@ cudaError_t dispatch_d(const float* xsT, int n, int np, int dp, int cap, int lst
 #define COSTAL_D(D)                                                                                            \
     case D:                                                                                                    \
         return launch_one<S, D>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor, \
+                                tnorm, cand_idx, cand_score, tau, st);
+    if (tnorm)
+        return launch_one<S, 0>(xsT, n, np, dp, cap, lstride, qlist, qcount, segs, grid_rows, part_stride, tfloor,
                                 tnorm, cand_idx, cand_score, tau, st);
     switch (dp) {
         COSTAL_D(8) COSTAL_D(16) COSTAL_D(24) COSTAL_D(32) COSTAL_D(40) COSTAL_D(48) COSTAL_D(56) COSTAL_D(64)
