@@ -133,6 +133,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, device="cpu"):
+    """The largest x over all ranks of the initialised process group (a job's time is its slowest
+    rank's); x itself without one. Every rank must call it."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_cells_per_s(n, ws, ms):
+    """Whole-job throughput of ws replicas that each build the graph of n cells in (at most) ms."""
+    return ws * n / (ms / 1e3)
+
+
 def cpu_baseline(x, wl, target_s=15.0, threads=0):
     """The oracle's blocked CPU path on a bounded sample of query rows against all n columns, sized
     to about `target_s` seconds of CPU work. Returns (cells/s, cores, sample description)."""
@@ -291,11 +309,8 @@ def main():
             stats.append(st.as_dict())
         launches = lib.costal_launch_count() - l0
         torch.cuda.synchronize()
-        ms = float(np.mean(times))
+        ms = max_over_ranks(float(np.mean(times)), "cuda")
         if ws > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
             dist.barrier()
         return ms, stats, launches, int(m.value)
 
@@ -327,11 +342,7 @@ def main():
         t = time.perf_counter()
         step_host()
         e2e_t.append(time.perf_counter() - t)
-    e2e_s = float(np.mean(e2e_t))
-    if ws > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(float(np.mean(e2e_t)), "cuda")
     # parity guard: the timed host result equals the device-resident one
     assert int(m2.value) == edges
     host_edges = (h_rows[:edges].numpy().copy(), h_cols[:edges].numpy().copy(), h_w[:edges].numpy().copy())
@@ -342,7 +353,7 @@ def main():
         pms, pstats, _, pedges = timed_device(make_opts("fp32", False), 1, args.plain_steps)
         same = pedges == edges and all(
             np.array_equal(a, b.cpu().numpy()[:edges]) for a, b in zip(host_edges, (d_rows, d_cols, d_w)))
-        plain = {"ms_per_step": pms, "value": ws * n / (pms * 1e-3), "unit": "cells/s", "steps": args.plain_steps,
+        plain = {"ms_per_step": pms, "value": job_cells_per_s(n, ws, pms), "unit": "cells/s", "steps": args.plain_steps,
                  "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in pstats])),
                  "speedup": pms / ms, "identical_edges": bool(same)}
 
@@ -350,7 +361,7 @@ def main():
     stop_only = None
     if learned:
         sms, sstats, _, sedges = timed_device(make_opts("bf16", False), 1, args.steps)
-        stop_only = {"ms_per_step": sms, "value": ws * n / (sms * 1e-3), "unit": "cells/s", "steps": args.steps,
+        stop_only = {"ms_per_step": sms, "value": job_cells_per_s(n, ws, sms), "unit": "cells/s", "steps": args.steps,
                      "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in sstats])),
                      "blocks_stopped": sstats[-1]["blocks_stopped"], "same_edge_count": sedges == edges}
         if plain is not None:
@@ -384,7 +395,7 @@ def main():
         traffic = traffic_per_launch(args.backend, pairs, d)
         line = {
             "metric": METRIC,
-            "value": ws * n / (ms * 1e-3),
+            "value": job_cells_per_s(n, ws, ms),
             "unit": "cells/s",
             "n_gpus": ws,
             "steps": args.steps,
@@ -399,7 +410,7 @@ def main():
             "config": {"workload": wl.name, "n": n, "d": d, "k": k, "margin": wl.margin, "backend": args.backend,
                        "learned_prune": learned, "weight": "tanimoto",
                        "l2": "flushed between steps (512 MB write outside the timed events)"},
-            "e2e": {"value": ws * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
+            "e2e": {"value": job_cells_per_s(n, ws, e2e_s * 1e3), "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
                     "d2h_bytes_per_step": edges * 16},
             "gpu_launches": int(launches),
             "gpu_launches_per_step": launches / args.steps,
@@ -420,7 +431,7 @@ def main():
             "clocks": clocks.summary(),
         }
         if train is not None:
-            line["value_incl_training"] = ws * n / ((ms + train["ms_labels"] + train["ms_train"]) * 1e-3)
+            line["value_incl_training"] = job_cells_per_s(n, ws, ms + train["ms_labels"] + train["ms_train"])
         if not args.no_cpu:
             v, cores, sample = cpu_baseline(x, wl, target_s=args.cpu_seconds)
             line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample}
