@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(PREP_ROWS) k_prep(const float* __restrict__ x,
         if (r < np) {
             for (int tt = 0; tt < tend; ++tt) {
                 float v = 0.0f;
-                if (r < n && t0 + tt < d) v = (float)((double)tile[threadIdx.x * (PREP_TCHUNK + 1) + tt] * inv);
+                if (r < n && t0 + tt < d) v = (float)(f64_of(tile[threadIdx.x * (PREP_TCHUNK + 1) + tt]) * inv);
                 xsT[(size_t)(t0 + tt) * np + r] = v;
             }
         }

@@ -758,10 +758,11 @@ __global__ void __launch_bounds__(SPLIT_ROWS)
             rb[d + t] = hb;
             rb[2 * d + t] = lb;
         }
-        sh = __fma_rn((double)h, (double)h, sh);
-        sl = __fma_rn((double)l, (double)l, sl);
-        sr = __fma_rn((double)rem, (double)rem, sr);
-        const double p = (double)h + (double)l;
+        const double h64 = f64_of(h), l64 = f64_of(l), r64 = f64_of(rem);  // exact widenings
+        sh = __fma_rn(h64, h64, sh);
+        sl = __fma_rn(l64, l64, sl);
+        sr = __fma_rn(r64, r64, sr);
+        const double p = h64 + l64;
         sp = __fma_rn(p, p, sp);
     }
     const double v[4] = {sqrt(sh), sqrt(sl), sqrt(sr), sqrt(sp)};
@@ -819,10 +820,11 @@ __global__ void __launch_bounds__(256)
         rb[t] = hb;
         rb[d + t] = hb;
         rb[2 * d + t] = lb;
-        sh = __fma_rn((double)h, (double)h, sh);
-        sl = __fma_rn((double)l, (double)l, sl);
-        sr = __fma_rn((double)rem, (double)rem, sr);
-        const double p = (double)h + (double)l;
+        const double h64 = f64_of(h), l64 = f64_of(l), r64 = f64_of(rem);  // exact widenings
+        sh = __fma_rn(h64, h64, sh);
+        sl = __fma_rn(l64, l64, sl);
+        sr = __fma_rn(r64, r64, sr);
+        const double p = h64 + l64;
         sp = __fma_rn(p, p, sp);
     }
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
