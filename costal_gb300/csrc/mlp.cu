@@ -40,25 +40,24 @@ __host__ __device__ inline Off offsets(int F) {
 
 // ---- features ---------------------------------------------------------------------------------
 // One warp per row: the row's (at most 64) coordinates loaded once, two per lane, and broadcast by
-// shuffles; 8 centroid cosines per lane; a branch-free warp bitonic sort of the 256 cosines
-// (descending; only the values are kept, so ties need no order), the first 64 kept. Centroids sit
-// in shared memory with an odd row stride, so the lanes' reads of 32 different centroids hit 32
-// different banks.
+// shuffles; lane L takes the 8 consecutive centroids 8L … 8L + 7, read as two 16-byte words per
+// dimension from a transposed shared copy laid out so that a warp's words are contiguous (no bank
+// conflicts); then a branch-free warp bitonic sort of the 256 cosines (descending; only the values
+// are kept, so ties need no order) in which strides below 8 stay in a lane's registers, and the first
+// 64 (lanes 0-7) are kept. Each cosine is the same FMA chain over the dimensions in order.
 
-// Bitonic sort of a warp-distributed array of floats (position p = s·32 + lane), descending.
-template <int SL>
-__device__ __forceinline__ void warp_sort_desc(float (&v)[SL], int lane) {
-    constexpr int N = 32 * SL;
+// Bitonic sort of a warp-distributed array, lane-major (position p = 8·lane + s), descending.
+__device__ __forceinline__ void warp_sort_desc_lane8(float (&v)[8], int lane) {
 #pragma unroll
-    for (int size = 2; size <= N; size <<= 1) {
+    for (int size = 2; size <= 256; size <<= 1) {
 #pragma unroll
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (stride >= 32) {
+            if (stride < 8) {
 #pragma unroll
-                for (int s = 0; s < SL; ++s) {
-                    const int t = s ^ (stride >> 5);
+                for (int s = 0; s < 8; ++s) {
+                    const int t = s ^ stride;
                     if (t > s) {
-                        const bool desc = ((s * 32 + lane) & size) == 0;
+                        const bool desc = ((8 * lane + s) & size) == 0;
                         const float hi = fmaxf(v[s], v[t]), lo = fminf(v[s], v[t]);
                         v[s] = desc ? hi : lo;
                         v[t] = desc ? lo : hi;
@@ -66,9 +65,10 @@ __device__ __forceinline__ void warp_sort_desc(float (&v)[SL], int lane) {
                 }
             } else {
 #pragma unroll
-                for (int s = 0; s < SL; ++s) {
-                    const float o = __shfl_xor_sync(COSTAL_FULL_MASK, v[s], stride);
-                    const bool keep_max = ((lane & stride) == 0) == (((s * 32 + lane) & size) == 0);
+                for (int s = 0; s < 8; ++s) {
+                    const float o = __shfl_xor_sync(COSTAL_FULL_MASK, v[s], stride >> 3);
+                    const int p = 8 * lane + s;
+                    const bool keep_max = ((p & stride) == 0) == ((p & size) == 0);
                     v[s] = keep_max ? fmaxf(v[s], o) : fminf(v[s], o);
                 }
             }
@@ -76,11 +76,20 @@ __device__ __forceinline__ void warp_sort_desc(float (&v)[SL], int lane) {
     }
 }
 
+constexpr int FEAT_C = 256;  // centroid slots of the feature kernel (K ≤ 256)
+
 __global__ void k_features(const float* __restrict__ xsT, int np, int d, const float* __restrict__ cent, int K,
                            const uint32_t* __restrict__ rows, int m, float* __restrict__ feat) {
-    extern __shared__ float c_s[];  // [K][ds]
-    const int ds = d | 1;
-    for (int e = threadIdx.x; e < K * d; e += blockDim.x) c_s[(e / d) * ds + e % d] = cent[e];
+    // [d][256]: for dimension t, word h (0, 1) of lane L sits at t·256 + 128·h + 4·L, holding centroids
+    // 8L + 4h … 8L + 4h + 3 (zero past K)
+    extern __shared__ float4 c_s4[];
+    float* c_s = reinterpret_cast<float*>(c_s4);
+    for (int e = threadIdx.x; e < d * FEAT_C; e += blockDim.x) {
+        const int t = e / FEAT_C, q = e % FEAT_C;
+        const int h = q >> 7, L = (q & 127) >> 2, j = q & 3;
+        const int c = 8 * L + 4 * h + j;
+        c_s[e] = c < K ? cent[(size_t)c * d + t] : 0.0f;
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int F = d + MLP_TOPC;
@@ -95,21 +104,27 @@ __global__ void k_features(const float* __restrict__ xsT, int np, int d, const f
         for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
         for (int t = 0; t < d; ++t) {
             const float a = __shfl_sync(COSTAL_FULL_MASK, t < 32 ? x0 : x1, t & 31);
-#pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                const int c = s * 32 + lane;
-                if (c < K) dot[s] = fmaf(a, c_s[c * ds + t], dot[s]);
-            }
+            const float4 w0 = c_s4[t * (FEAT_C / 4) + lane], w1 = c_s4[t * (FEAT_C / 4) + 32 + lane];
+            dot[0] = fmaf(a, w0.x, dot[0]);
+            dot[1] = fmaf(a, w0.y, dot[1]);
+            dot[2] = fmaf(a, w0.z, dot[2]);
+            dot[3] = fmaf(a, w0.w, dot[3]);
+            dot[4] = fmaf(a, w1.x, dot[4]);
+            dot[5] = fmaf(a, w1.y, dot[5]);
+            dot[6] = fmaf(a, w1.z, dot[6]);
+            dot[7] = fmaf(a, w1.w, dot[7]);
         }
 #pragma unroll
         for (int s = 0; s < 8; ++s)
-            if (s * 32 + lane >= K) dot[s] = -CUDART_INF_F;
-        warp_sort_desc<8>(dot, lane);
+            if (8 * lane + s >= K) dot[s] = -CUDART_INF_F;
+        warp_sort_desc_lane8(dot, lane);
         float* f = feat + (size_t)i * F;
         if (lane < d) f[lane] = x0;
         if (lane + 32 < d) f[lane + 32] = x1;
-        f[d + lane] = dot[0];
-        f[d + 32 + lane] = dot[1];
+        if (lane < MLP_TOPC / 8) {
+#pragma unroll
+            for (int s = 0; s < 8; ++s) f[d + 8 * lane + s] = dot[s];
+        }
     }
 }
 
@@ -375,7 +390,8 @@ static size_t grad_smem(int F) { return (size_t)(R * F + 4 * R * T + 2 * R) * 4;
 cudaError_t features(const float* xsT, int np, int d, const float* centroids, int K, const uint32_t* rows, int m,
                      float* feat, cudaStream_t st) {
     if (m == 0) return cudaSuccess;
-    const size_t smem = (size_t)K * (d | 1) * 4;
+    if (K > FEAT_C) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)d * FEAT_C * 4;
     cudaError_t e = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;

@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(KM_BLOCK) k_assign(const float* __restrict__ r
     assign[i] = arg;
 }
 
-// One CTA per centroid: the normalised sum of its rows. Thread t adds rows t, t+128, … in order,
-// then the 128 partial sums are combined by a fixed tree: deterministic. An empty cluster keeps its
+// One CTA per centroid: the normalised sum of its rows. Thread t adds rows 4t … 4t+3, then 512 on,
+// in order, then the 128 partial sums are combined by a fixed tree: deterministic. An empty cluster keeps its
 // previous centroid.
 constexpr int UPD_T = 128;
 __global__ void __launch_bounds__(UPD_T) k_centroid_update(const float* __restrict__ rows, int m, int d,
@@ -99,14 +99,23 @@ __global__ void __launch_bounds__(UPD_T) k_centroid_update(const float* __restri
 #pragma unroll
     for (int t = 0; t < 64; ++t) acc[t] = 0.0f;
     int cnt = 0;
-    for (int i = threadIdx.x; i < m; i += UPD_T) {
-        if (assign[i] == (uint32_t)c) {
-            ++cnt;
+    auto add_row = [&](int i) {
+        ++cnt;
 #pragma unroll
-            for (int t = 0; t < 64; ++t)
-                if (t < d) acc[t] += rows[(size_t)i * d + t];
-        }
+        for (int t = 0; t < 64; ++t)
+            if (t < d) acc[t] += rows[(size_t)i * d + t];
+    };
+    // four assignments per 16-byte load (the array is 256-byte aligned), then the tail
+    const int m4 = m & ~3;
+    for (int i4 = 4 * threadIdx.x; i4 < m4; i4 += 4 * UPD_T) {
+        const uint4 a = *reinterpret_cast<const uint4*>(assign + i4);
+        if (a.x == (uint32_t)c) add_row(i4);
+        if (a.y == (uint32_t)c) add_row(i4 + 1);
+        if (a.z == (uint32_t)c) add_row(i4 + 2);
+        if (a.w == (uint32_t)c) add_row(i4 + 3);
     }
+    for (int i = m4 + threadIdx.x; i < m; i += UPD_T)
+        if (assign[i] == (uint32_t)c) add_row(i);
 #pragma unroll
     for (int t = 0; t < 64; ++t)
         if (t < d) part[threadIdx.x][t] = acc[t];
