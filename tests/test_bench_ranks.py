@@ -1,5 +1,6 @@
-"""The multi-rank side of bench.py on the CPU (gloo, two ranks): every rank reports the slowest
-rank's time, and the job's throughput counts the cells of every replica. No GPU needed."""
+"""bench.py's host logic on the CPU: the multi-rank side (gloo, two ranks: every rank reports the slowest
+rank's time, and the job's throughput counts the cells of every replica) and the DRAM-traffic estimate
+from the committed ncu captures. No GPU needed."""
 
 import os
 import socket
@@ -54,3 +55,21 @@ def test_single_process_and_job_throughput():
     # two replicas of 1,000 cells, the slower one in 15 ms: 2 · 1000 / 0.015 cells/s
     assert bench.job_cells_per_s(1000, 2, 15.0) == pytest.approx(2 * 1000 / 0.015)
     assert bench.job_cells_per_s(2_000_000, 1, 250.0) == pytest.approx(8_000_000.0)
+
+
+def test_traffic_estimate_from_the_committed_captures():
+    import json
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    table = json.loads((ROOT / "profiles" / "dram_traffic.json").read_text())
+    pairs = 1e9
+    # resident tensor-core form (3d <= 128): bytes per computed pair
+    assert bench.traffic_per_launch("bf16", pairs, 40) == pytest.approx(table["bf16"]["bytes_per_pair"] * pairs)
+    # K loop (3d > 128): bytes per pair per padded K
+    kp = (3 * 2000 + 63) // 64 * 64
+    assert bench.traffic_per_launch("bf16", pairs, 2000) == pytest.approx(
+        table["bf16_kloop"]["bytes_per_pair_per_k"] * kp * pairs)
+    assert bench.traffic_per_launch("fp32", pairs, 40) == pytest.approx(table["fp32"]["bytes_per_pair"] * pairs)
+    assert bench.traffic_per_launch("no-such-backend", pairs, 40) is None
