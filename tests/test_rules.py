@@ -60,3 +60,35 @@ def test_integer_widening_restated_on_every_class():
     pats = pats[(pats & 0x7F800000) != 0x7F800000]  # finite only
     want = pats.view(np.float32).astype(np.float64).view(np.uint64)
     np.testing.assert_array_equal(f64_of(pats), want)
+
+
+@pytest.mark.parametrize("d", [1, 5, 16, 40, 64, 300])
+def test_coarse_tanimoto_stays_within_its_bound(d):
+    # The GPU's coarse Tanimoto score: T = dot / (A + B − dot), dot = a·b·ĉ with ĉ the f32 dot of the
+    # f32-normalised rows and a, A the f32 norm and squared norm; within 2(d+12)·2⁻²³ of the exact T.
+    rng = np.random.default_rng(d)
+    n = 400
+    x = rng.normal(size=(n, d)) * rng.uniform(0.01, 100.0, size=(n, 1))
+    x[rng.random(x.shape) < 0.3] = 0.0
+    x = x.astype(np.float32)
+    x64 = x.astype(np.float64)
+    nrm = np.sqrt((x64 * x64).sum(1))
+    xs = np.where(nrm[:, None] > 0, x64 * (1.0 / np.where(nrm > 0, nrm, 1.0))[:, None], 0.0).astype(np.float32)
+    i = rng.integers(0, n, 20000)
+    j = rng.integers(0, n, 20000)
+    dot64 = (x64[i] * x64[j]).sum(1)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        cos = np.where((nrm[i] > 0) & (nrm[j] > 0), dot64 / (nrm[i] * nrm[j]), 0.0)
+        d_ex = nrm[i] * nrm[j] * cos
+        t_ex = np.where(d_ex == 0, 0.0, d_ex / (nrm[i] ** 2 + nrm[j] ** 2 - d_ex))
+    c32 = np.zeros(len(i), np.float32)
+    for t in range(d):  # one rounding per step, like the GPU's FMA chain within the (d+4)·2⁻²³ bound
+        c32 = (c32 + xs[i, t] * xs[j, t]).astype(np.float32)
+    a = nrm.astype(np.float32)
+    sq = (nrm * nrm).astype(np.float32)
+    dn = (a[i] * a[j]).astype(np.float32) * c32
+    den = (sq[i] + sq[j]).astype(np.float32) - dn
+    with np.errstate(invalid="ignore", divide="ignore"):
+        t32 = np.where((dn == 0) | (den <= 0), np.float32(0), dn / den).astype(np.float64)
+    bound = 2.0 * (d + 12) * 2.0 ** -23
+    assert np.abs(t32 - t_ex).max() <= bound
