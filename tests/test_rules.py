@@ -92,3 +92,50 @@ def test_coarse_tanimoto_stays_within_its_bound(d):
         t32 = np.where((dn == 0) | (den <= 0), np.float32(0), dn / den).astype(np.float64)
     bound = 2.0 * (d + 12) * 2.0 ** -23
     assert np.abs(t32 - t_ex).max() <= bound
+
+
+def bf16_rne(v32):
+    """f32 → bf16 (round to nearest even), returned as f32 values."""
+    u = np.asarray(v32, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32)
+
+
+def to_f32_toward_zero(x64):
+    f = x64.astype(np.float32)
+    away = np.abs(f.astype(np.float64)) > np.abs(x64)
+    f[away] = np.nextafter(f[away], np.float32(0))
+    return f
+
+
+@pytest.mark.parametrize("d", [3, 15, 40, 64, 200])
+def test_split_bf16_coarse_score_within_its_row_bound(d):
+    # The split A = [hi | lo | hi], B = [hi | hi | lo] and the per-row bound E_i of k_row_eps, against an
+    # accumulation model worse than the hardware's: products of each 16-wide step summed exactly, then
+    # truncated to f32, and the f32 accumulator truncated after every step.
+    rng = np.random.default_rng(100 + d)
+    n = 300
+    x = rng.normal(size=(n, d)) + rng.normal(0, 3, size=(1, d))
+    x64 = x / np.linalg.norm(x, axis=1, keepdims=True)
+    a = x64.astype(np.float32)
+    hi = bf16_rne(a)
+    lo = bf16_rne((a - hi).astype(np.float32))
+    rem = ((a - hi).astype(np.float32) - lo).astype(np.float64)
+    h64, l64 = hi.astype(np.float64), lo.astype(np.float64)
+    nh, nl, nr = (np.linalg.norm(v, axis=1) for v in (h64, l64, rem))
+    npn = np.linalg.norm(h64 + l64, axis=1)
+    Mh, Ml, Mr, Mp = nh.max(), nl.max(), nr.max(), npn.max()
+    K = 3 * d
+    split = nl * Ml + npn * Mr + nr * Mp + nr * Mr
+    acc = (K + 16) * 2.0 ** -21 * (nh * Mh + nl * Mh + nh * Ml)
+    E = split + acc + 2.0001 * 2.0 ** -24 + (d + 8) * 2.0 ** -52
+    A = np.concatenate([h64, l64, h64], 1)
+    B = np.concatenate([h64, h64, l64], 1)
+    i = rng.integers(0, n, 3000)
+    j = rng.integers(0, n, 3000)
+    accum = np.zeros(len(i), np.float32)
+    for k0 in range(0, K, 16):
+        step = (A[i, k0:k0 + 16] * B[j, k0:k0 + 16]).sum(1)  # exact enough in f64 for bf16 products
+        accum = to_f32_toward_zero(accum.astype(np.float64) + to_f32_toward_zero(step).astype(np.float64))
+    exact = (x64[i] * x64[j]).sum(1)
+    assert (np.abs(accum.astype(np.float64) - exact) <= E[i]).all()
