@@ -287,7 +287,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             CK(cudaStreamSynchronize(s));
             const int nfail = (int)c.h_misc->tc_fail_count;
             if (nfail > 0) {
-                const int segs = coarse_fp32_segments(nfail, np, cap, c.sm_count);
+                const int segs = coarse_fp32_segments(nfail, np, c.sm_count);
                 if (segs > 1) {
                     CK(ensure(c.part_idx, (size_t)segs * nfail * cap * 4));
                     CK(ensure(c.part_score, (size_t)segs * nfail * cap * 4));

@@ -635,7 +635,7 @@ cudaError_t launch_coarse_fp32_tanimoto(const float* xsT, int n, int np, int dp,
                              tau, st);
 }
 
-int coarse_fp32_segments(int count, int np, int cap, int sm_count) {
+int coarse_fp32_segments(int count, int np, int sm_count) {
     // enough CTAs for two per SM; the merge reads segs · cap entries per row, 256 − cap at a time
     const int qblocks = (count + plain::BM - 1) / plain::BM, all = np / plain::BN;
     int segs = (2 * sm_count + qblocks - 1) / qblocks;

@@ -21,7 +21,7 @@ cudaError_t launch_coarse_fp32(const float* xsT, int n, int np, int dp, int cap,
                                cudaStream_t st);
 // Few listed rows: the columns split into `segs` segments (one CTA per 128 rows per segment), their
 // lists merged per row. part_* hold segs × count × cap entries (τ: segs × count).
-int coarse_fp32_segments(int count, int np, int cap, int sm_count);
+int coarse_fp32_segments(int count, int np, int sm_count);
 // tfloor (optional, by row): a per-row threshold below which no column can be among the best cap.
 cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, int cap, int lstride,
                                      const uint32_t* qlist, const unsigned* qcount, int count, int segs,
