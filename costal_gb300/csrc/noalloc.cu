@@ -8,7 +8,10 @@
 // other allocating routine.
 //
 // The price: the array (NOALLOC_SCRATCH_BYTES, 16 MiB) is reserved on every GPU that loads the
-// library, for as long as the process lives, and it is shared by all calls. It holds the row-sorted
+// library's device code, for as long as the process lives, and it is shared by all calls. With CUDA's
+// lazy module loading (the default) that reservation is made when the device code is first used on a
+// device, which may be this entry point's first call there: on a device without 16 MiB free that call
+// fails with COSTAL_ECUDA. A caller with a fixed budget makes one call at start-up. It holds the row-sorted
 // copy of the neighbour matrix, so n·k may be at most NOALLOC_MAX_ENTRIES; larger inputs are rejected
 // before any device work. Two calls whose work overlaps on the GPU (different streams, or host
 // threads) race on the array and corrupt each other's result: serialise them.
@@ -93,12 +96,13 @@ void put_err(char* err, size_t errlen, const std::string& msg) {
 
 extern "C" int costal_reweight_jaccard_device_noalloc(const int32_t* d_idx, uint64_t n, uint32_t k, double* d_out,
                                                       void* stream, char* err, size_t errlen) {
-    const uint64_t nk = n * (uint64_t)k;
-    if (nk == 0) return COSTAL_OK;
-    if (n > (uint64_t)INT32_MAX || nk > NOALLOC_MAX_ENTRIES) {
+    if (n == 0 || k == 0) return COSTAL_OK;
+    // Each factor is checked before the product is formed, so n * k cannot wrap around.
+    if (n > NOALLOC_MAX_ENTRIES || k > NOALLOC_MAX_ENTRIES || n * (uint64_t)k > NOALLOC_MAX_ENTRIES) {
         put_err(err, errlen,
-                "costal_reweight_jaccard_device_noalloc: n*k = " + std::to_string(nk) + " exceeds the fixed scratch of " +
-                    std::to_string(NOALLOC_MAX_ENTRIES) + " neighbour entries; use costal_reweight instead");
+                "costal_reweight_jaccard_device_noalloc: n*k = " + std::to_string(n) + "*" + std::to_string(k) +
+                    " exceeds the fixed scratch of " + std::to_string(NOALLOC_MAX_ENTRIES) +
+                    " neighbour entries; use costal_reweight instead");
         return COSTAL_EINVAL;
     }
     int dev = 0;

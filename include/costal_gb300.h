@@ -128,7 +128,10 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
  * a fixed 16 MiB array compiled into the library (reserved on every GPU that loads it, until the process
  * exits), so n*k is limited to 4,194,304 neighbour entries; larger inputs return COSTAL_EINVAL before any
  * device work. The first call on a device looks up that array's address (make it before any stream
- * capture). All calls share the array: calls that overlap on the GPU race and must be serialised. */
+ * capture); under CUDA's lazy module loading that first call may also be when the 16 MiB is reserved,
+ * and it fails with COSTAL_ECUDA on a device without that much free, so a caller with a fixed budget
+ * makes it at start-up. All calls share the array: calls that overlap on the GPU race and must be
+ * serialised. */
 int costal_reweight_jaccard_device_noalloc(const int32_t* d_idx, uint64_t n, uint32_t k, double* d_out, void* stream,
                                            char* err, size_t errlen);
 

@@ -49,6 +49,39 @@ def test_noalloc_jaccard_matches_reweight_twice_in_a_row(ext):
         np.testing.assert_array_equal(d_out.cpu().numpy(), want)
 
 
+def test_noalloc_allocates_nothing_and_holds_its_stated_maximum(ext, oracle):
+    """At n*k exactly the scratch's capacity the result equals the oracle's Jaccard (weight.rs:64-92),
+    and the device's free memory does not move across calls: the library allocates nothing."""
+    torch = pytest.importorskip("torch")
+    from costal_gb300 import _lib as L
+
+    lib = L.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    n, k = MAX_ENTRIES // 16, 16
+    rng = np.random.default_rng(5)
+    idx = rng.integers(0, n, size=(n, k), dtype=np.int32)
+    want = oracle.reweight(idx.view(np.uint32), np.zeros((n, k)), np.ones(n), "jaccard")
+    d_idx = torch.from_numpy(idx).cuda()
+    d_out = torch.full((n, k), float("nan"), dtype=torch.float64, device="cuda")
+    rc, msg = call_noalloc(lib, d_idx, n, k, d_out, stream)  # warm-up: the module is loaded by now
+    assert rc == 0, msg
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        d_out.fill_(float("nan"))
+        rc, msg = call_noalloc(lib, d_idx, n, k, d_out, stream)
+        assert rc == 0, msg
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(d_out.cpu().numpy(), want)
+    assert torch.cuda.mem_get_info()[0] == free_before
+    # one entry more than the scratch holds is refused before any device work
+    rc, msg = call_noalloc(lib, d_idx, MAX_ENTRIES + 1, 1, d_out, stream)
+    assert rc == L.COSTAL_EINVAL and "exceeds the fixed scratch" in msg
+    # a product that would wrap around 64 bits is refused too, not taken for an empty input
+    rc, msg = call_noalloc(lib, d_idx, 1 << 62, 4, d_out, stream)
+    assert rc == L.COSTAL_EINVAL and "exceeds the fixed scratch" in msg
+
+
 def test_noalloc_rejects_what_it_cannot_hold(ext):
     torch = pytest.importorskip("torch")
     from costal_gb300 import _lib as L
