@@ -15,11 +15,16 @@ Differences from the reference, all documented:
     change the GPU tiling (the reference: they change speed only, knn.rs:39-44). `prune` (speed
     only, as in the reference) switches the exact early stop of the bf16 backend's block lists.
   - k + margin above 128 raises NotImplementedError (the GPU keeps at most 128 candidates a row).
+  - The backend used when a caller passes no `matmul` (as costal.knn and costal.find_communities of the
+    reference package never do) is DEFAULT_MATMUL: "fp32" unless the environment variable
+    COSTAL_GB300_MATMUL names another backend when this module is imported. Setting it to "bf16" moves
+    an unchanged caller onto the certified tensor-core path; the output stays the same bits.
 """
 
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -72,7 +77,21 @@ def row_l2_norms(x):
 
 
 _SELECT_NAMES = ("cosine", "tanimoto")
-_BACKENDS = {None: L.BACKEND_FP32, "fp32": L.BACKEND_FP32, "gemm": L.BACKEND_FP32, "bf16": L.BACKEND_BF16}
+_BACKENDS = {"fp32": L.BACKEND_FP32, "gemm": L.BACKEND_FP32, "bf16": L.BACKEND_BF16}
+
+DEFAULT_MATMUL = os.environ.get("COSTAL_GB300_MATMUL", "fp32")
+if DEFAULT_MATMUL not in _BACKENDS:
+    raise ImportError(f'COSTAL_GB300_MATMUL="{DEFAULT_MATMUL}" is not a backend of this library ({", ".join(_BACKENDS)})')
+
+
+def _backend(matmul):
+    """The backend name a call runs on: its `matmul`, or DEFAULT_MATMUL when it names none."""
+    name = DEFAULT_MATMUL if matmul is None else matmul
+    if name == "accelerate":
+        raise ValueError("matmul backend accelerate is not available on this platform")  # knn.rs:120-122
+    if name not in _BACKENDS:
+        raise ValueError(f'unknown matmul backend "{name}"')
+    return name
 
 
 def _parse_select(select):
@@ -112,10 +131,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
     n, d = x.shape
     if n > np.iinfo(np.int32).max:
         raise ValueError(f"n={n} exceeds the int32 index range")
-    if matmul == "accelerate":
-        raise ValueError("matmul backend accelerate is not available on this platform")  # knn.rs:120-122
-    if matmul not in _BACKENDS:
-        raise ValueError(f'unknown matmul backend "{matmul}"')
+    matmul = _backend(matmul)
     for name, v in (("k", k), ("margin", margin), ("row_block", row_block), ("col_block", col_block),
                     ("n_threads", n_threads)):
         _check_knob(name, v)
@@ -131,7 +147,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
         "fallback_rows": int(st.fallback_rows),
         "row_block": int(st.row_block),
         "col_block": int(st.col_block),
-        "matmul": "bf16" if matmul == "bf16" else ("gemm" if matmul == "gemm" else "fp32"),
+        "matmul": matmul,
         "margin": int(st.margin),
         "select": sel,
         "blocks_skipped": int(st.blocks_skipped),
@@ -140,6 +156,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
         "recomputed_rows": int(st.recomputed_rows),
         "pruned_fallback_rows": int(st.pruned_fallback_rows),
         "max_coarse_err": float(st.max_coarse_err),
+        "max_err_ratio": float(st.max_err_ratio),
         "blocks_stopped": int(st.blocks_stopped),
         "ms_order": float(st.ms_order),
         "ms_coarse": float(st.ms_coarse),
@@ -207,8 +224,7 @@ def _build_graph(x, k, *, weight="tanimoto", margin=None, matmul=None, return_kn
     x = _arr(x, np.float32, 2, "x")
     n, d = x.shape
     wc = _weight_code(weight)
-    if matmul not in _BACKENDS:
-        raise ValueError(f'unknown matmul backend "{matmul}"')
+    matmul = _backend(matmul)
     k = int(k)
     rows = np.empty(n * k, np.int32)
     cols = np.empty(n * k, np.int32)
@@ -238,8 +254,7 @@ def _build_graph_csr(x, k, *, weight="tanimoto", margin=None, matmul=None, learn
     x = _arr(x, np.float32, 2, "x")
     n, d = x.shape
     wc = _weight_code(weight)
-    if matmul not in _BACKENDS:
-        raise ValueError(f'unknown matmul backend "{matmul}"')
+    matmul = _backend(matmul)
     k = int(k)
     indptr = np.empty(n + 1, np.uint64)
     nbr = np.empty(2 * n * k, np.uint32)
@@ -364,8 +379,8 @@ def tile_budget_bytes() -> int:
 
 
 def default_matmul() -> str:
-    """lib.rs:442-446: name of the default coarse-pass backend."""
-    return "fp32"
+    """lib.rs:442-446: name of the default coarse-pass backend (DEFAULT_MATMUL)."""
+    return DEFAULT_MATMUL
 
 
 # ---- the learned block-pruning model (GB300 addition; no counterpart in the reference) ----------

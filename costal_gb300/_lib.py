@@ -57,6 +57,7 @@ class KnnStats(C.Structure):
         ("ms_order", C.c_double),
         ("ms_kernel", C.c_double),
         ("blocks_stopped", C.c_uint64),
+        ("max_err_ratio", C.c_double),
     ]
 
     def as_dict(self):

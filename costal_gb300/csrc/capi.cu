@@ -42,7 +42,7 @@ struct DevBuf {
 
 struct Misc {  // small device-side results read back at the end of a call
     unsigned long long bad_row;
-    unsigned long long max_err_bits;
+    unsigned long long max_err_bits[2];  // max |coarse − rescored|, and its max ratio to the row's bound
     unsigned long long first_bad_idx;
     unsigned fb_count;
     unsigned m;
@@ -226,7 +226,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
                           c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps_t, cap < n - 1, 1, nullptr,
                           nullptr, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
-                          &dm->fb_count, &dm->max_err_bits, s));
+                          &dm->fb_count, dm->max_err_bits, s));
         CK(cudaEventRecord(c.ev[3], s));
         if (cap < n - 1) {
             if (gather_smem(k, d, dp) > 227 * 1024)
@@ -278,7 +278,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                               c.tau.as<float>(), d_norms, plan.row_eps, learned ? pp.row_ub : nullptr,
                               &dm->prune_fail_count, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx, d_cos, d_w,
                               c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
-                              &dm->max_err_bits, s));
+                              dm->max_err_bits, s));
             if (coarse_fp32_smem(dp, cap) > 227 * 1024)
                 throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 re-run of uncertified rows"};
             // How many rows failed decides the re-run's shape (few rows: the columns split across CTAs).
@@ -316,7 +316,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
                               c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0, nullptr,
                               nullptr, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
-                              &dm->fb_count, &dm->max_err_bits, s));
+                              &dm->fb_count, dm->max_err_bits, s));
             CK(cudaEventRecord(c.ev[3], s));
         }
         if (cap < n - 1) {
@@ -345,8 +345,10 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         st->recomputed_rows = used_tc ? hm.tc_fail_count : 0;
         st->pruned_fallback_rows = hm.prune_fail_count;
         double me;
-        std::memcpy(&me, &hm.max_err_bits, 8);
+        std::memcpy(&me, &hm.max_err_bits[0], 8);
         st->max_coarse_err = me;
+        std::memcpy(&me, &hm.max_err_bits[1], 8);
+        st->max_err_ratio = me;
         st->ms_prep = elapsed(c.ev[0], c.ev[1]);
         st->ms_order = elapsed(c.ev[1], c.ev[5]);
         st->ms_coarse = elapsed(c.ev[5], c.ev[2]);

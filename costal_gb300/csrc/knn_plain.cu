@@ -282,7 +282,7 @@ __device__ __forceinline__ void rescore_group(int g, const float* __restrict__ x
     __syncthreads();
     // phase 1: the f64 rescoring of the packed entries
     const bool vec4 = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
-    double err = 0.0;
+    double err = 0.0, ratio = 0.0;
     for (int w = tid; w < total; w += blockDim.x) {
         const int code = work_s[w], r = code / RS_MAXCAP, p = code - r * RS_MAXCAP, e = r * cap + p;
         const int i = row_s[r];
@@ -305,17 +305,26 @@ __device__ __forceinline__ void rescore_group(int g, const float* __restrict__ x
         const double ni = norms[i], nj = norms[j];
         const double c = cos64(dot, ni, nj);
         const double score = select == 0 ? c : tani_from_cos(ni, nj, c);
-        err = fmax(err, fabs((double)cand_score[(size_t)i * lstride + p] - score));
+        const double diff = fabs((double)cand_score[(size_t)i * lstride + p] - score);
+        err = fmax(err, diff);
+        ratio = fmax(ratio, diff / (row_eps ? row_eps[i] : eps));  // against the bound the certificate used
         sc_s[e] = score;
         cs_s[e] = c;
         id_s[e] = j;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
-    // one address for the whole grid: read it first, so that only a new maximum pays for the atomic
+    for (int o = 16; o > 0; o >>= 1) {
+        err = fmax(err, __shfl_xor_sync(COSTAL_FULL_MASK, err, o));
+        ratio = fmax(ratio, __shfl_xor_sync(COSTAL_FULL_MASK, ratio, o));
+    }
+    // max_err_bits[0]: the largest |coarse − rescored|, [1]: the largest ratio of it to the row's bound
+    // (non-negative doubles order like their bits). One address for the whole grid: read it first,
+    // so that only a new maximum pays for the atomic.
     if (lane == 0 && max_err_bits && err > 0.0) {
         const unsigned long long eb = (unsigned long long)__double_as_longlong(err);
         if (eb > *reinterpret_cast<volatile unsigned long long*>(max_err_bits)) atomicMax(max_err_bits, eb);
+        const unsigned long long rb = (unsigned long long)__double_as_longlong(ratio);
+        if (rb > *reinterpret_cast<volatile unsigned long long*>(max_err_bits + 1)) atomicMax(max_err_bits + 1, rb);
     }
     __syncthreads();
     if (warp >= nr) return;  // no barrier below

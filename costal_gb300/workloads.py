@@ -51,8 +51,12 @@ def _mixture(rng, sizes, d, mean_sd=2.0, std_lo=0.3, std_hi=1.0):
     return out, means, stds
 
 
-def _shuffle(rng, x):
-    return np.ascontiguousarray(x[rng.permutation(len(x))])
+def _shuffle(rng, x, labels=None):
+    """Rows in a seeded random order; with `labels` (one per row), also those labels in that order."""
+    perm = rng.permutation(len(x))
+    if labels is None:
+        return np.ascontiguousarray(x[perm])
+    return np.ascontiguousarray(x[perm]), labels[perm]
 
 
 def mixture_20k(n=20_000, d=32, seed=0):
@@ -67,11 +71,14 @@ def rare_400k(n=400_000, d=15, seed=1):
     rare = max(1, round(n * 0.001))
     sizes = rng.multinomial(n - rare, np.full(12, 1 / 12))
     x, means, stds = _mixture(rng, sizes, d)
-    # the rare population: 3σ away from its nearest neighbouring cluster centre, along a random direction
+    # the rare population: centred 3σ (three of cluster c's standard deviations, along a random
+    # direction) from the centre of cluster c, which is then its nearest neighbouring cluster
     c = int(rng.integers(12))
     direction = rng.normal(size=d)
     direction /= np.linalg.norm(direction)
     centre = means[c] + 3.0 * stds[c] * direction
+    if int(np.argmin(np.linalg.norm(means - centre, axis=1))) != c:
+        raise ValueError("seed places the rare population nearer another cluster than the one it is offset from")
     r = centre + 0.5 * stds[c] * rng.standard_normal((rare, d))
     x = np.vstack([x, r.astype(np.float32)])
     return _shuffle(rng, np.arcsinh(x / 5.0).astype(np.float32))
@@ -111,12 +118,14 @@ def scrna_100k(n=100_000, d=2000, seed=3, chunk=10_000):
     return out
 
 
-def zipf_2m(n=2_000_000, d=40, seed=4):
+def zipf_2m(n=2_000_000, d=40, seed=4, return_labels=False):
+    """With return_labels, also each row's mixture component (0 = the largest of the 50)."""
     rng = np.random.default_rng(seed)
     w = 1.0 / np.arange(1, 51) ** 1.2
     sizes = rng.multinomial(n, w / w.sum())
     x, _, _ = _mixture(rng, sizes, d)
-    return _shuffle(rng, np.arcsinh(x / 5.0).astype(np.float32))
+    x, labels = _shuffle(rng, np.arcsinh(x / 5.0).astype(np.float32), np.repeat(np.arange(50), sizes))
+    return (x, labels) if return_labels else x
 
 
 GENERATORS = {

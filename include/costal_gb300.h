@@ -71,6 +71,9 @@ typedef struct costal_knn_stats {
     double ms_kernel;          /* the coarse tile + selection kernel alone (inside ms_coarse) */
     uint64_t blocks_stopped;   /* bf16 backend: list blocks left out because every row's threshold
                                   already exceeded their bound (exact; no certificate needed) */
+    double max_err_ratio;      /* max over the rescored candidates of |coarse - f64 score| divided by the
+                                  bound the row's certificate used (E_i on the bf16 backend, the FP32
+                                  epsilon otherwise): the certificate is sound while this stays below 1 */
 } costal_knn_stats;
 
 /* ---- module surface (crates/costal-py/src/lib.rs:80-102, 430-446) ---------------------------- */

@@ -51,6 +51,13 @@ def clustered(n, d, seed, n_centers=8, noise=0.5):
     return np.ascontiguousarray(x, dtype=np.float32)
 
 
+def scaled_clusters(n, d, seed):
+    """clustered() rows rescaled per row, so magnitude matters (the reference's tests/test_knn.py:97-102)."""
+    x = clustered(n, d, seed)
+    x *= np.random.default_rng(seed + 100).uniform(0.5, 3.0, size=(n, 1)).astype(np.float32)
+    return np.ascontiguousarray(x)
+
+
 class Lcg:
     """The reproducible generator of crates/costal-core/src/knn.rs:931-940 (its unit tests' data)."""
 
