@@ -24,8 +24,10 @@ inference and the block lists; the model itself is trained once before timing (r
   cpu_baseline — the oracle (C++ restatement of the reference's CPU path) on a bounded sample of
            query rows, all host threads.
 
-Multi-GPU (torchrun): every rank runs an independent replica of the workload on its own GPU
-(no collective on the data path); value = total cells of all ranks / max step time.
+Multi-GPU (torchrun, N > 1): the rows are split across the ranks (costal_gb300.shard): every rank
+holds all of X, computes its shard of the query rows against every column, the ranks all-gather the
+shards' neighbours, cosines and weights over NCCL, and every rank builds the fuzzy union; the total
+work is fixed at n ("strong" scaling) and value = n / the slowest rank's step time.
 """
 
 from __future__ import annotations
@@ -147,7 +149,8 @@ def max_over_ranks(x, device="cpu"):
 
 
 def job_cells_per_s(n, ws, ms):
-    """Whole-job throughput of ws replicas that each build the graph of n cells in (at most) ms."""
+    """Whole-job throughput: ws graphs of n cells each built in (at most) ms; the sharded benchmark
+    builds one graph of n cells across all ranks (ws = 1)."""
     return ws * n / (ms / 1e3)
 
 
@@ -190,7 +193,7 @@ def run_reference(args, wl, x):
     v = float(np.median(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": wl.n / v * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": wl.n / v * 1e3, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32 coarse + f64 rescoring", "data": "synthetic (seeded, shapes of the workload)",
         "config": {"workload": wl.name, "n": wl.n, "d": wl.d, "k": wl.k, "margin": wl.margin,
                    "l2": "inputs resident in host memory (CPU run)"},
@@ -280,7 +283,26 @@ def main():
     m = C.c_uint64()
     st = L.KnnStats()
 
+    sharded = ws > 1
+    shard_stats = {}
+
+    def step_sharded(o, xd):
+        from costal_gb300 import shard as S
+
+        (r, c, w), _, stt = S.build_graph_sharded(
+            xd, k, margin=wl.margin, matmul="bf16" if o.backend == L.BACKEND_BF16 else "fp32",
+            learned_prune=bool(o.learned_prune))
+        shard_stats.update(stt)
+        m.value = r.shape[0]
+        return r, c, w
+
     def step_device(o):
+        if sharded:
+            r, c, w = step_sharded(o, dx)
+            d_rows[: r.shape[0]].copy_(r)
+            d_cols[: c.shape[0]].copy_(c)
+            d_w[: w.shape[0]].copy_(w)
+            return
         rc = lib.costal_build_graph_device(C.c_void_p(dx.data_ptr()), n, d, k, C.byref(o), weight,
                                            C.c_void_p(d_rows.data_ptr()), C.c_void_p(d_cols.data_ptr()),
                                            C.c_void_p(d_w.data_ptr()), C.byref(m), C.byref(st),
@@ -306,7 +328,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
-            stats.append(st.as_dict())
+            stats.append(dict(shard_stats) if sharded else st.as_dict())
         launches = lib.costal_launch_count() - l0
         torch.cuda.synchronize()
         ms = max_over_ranks(float(np.mean(times)), "cuda")
@@ -326,6 +348,15 @@ def main():
     m2 = C.c_uint64()
 
     def step_host():
+        if sharded:  # X from pinned host memory to this rank's GPU, the sharded step, the edges back
+            xd = hx.to("cuda", non_blocking=True)
+            r, c, w = step_sharded(opts, xd)
+            e = r.shape[0]
+            h_rows[:e].copy_(r)
+            h_cols[:e].copy_(c)
+            h_w[:e].copy_(w)
+            m2.value = e
+            return
         rc = lib.costal_build_graph(C.c_void_p(hx.data_ptr()), n, d, k, C.byref(opts), weight,
                                     C.c_void_p(h_rows.data_ptr()), C.c_void_p(h_cols.data_ptr()),
                                     C.c_void_p(h_w.data_ptr()), C.byref(m2), None, None, None, None, err, errlen)
@@ -353,7 +384,7 @@ def main():
         pms, pstats, _, pedges = timed_device(make_opts("fp32", False), 1, args.plain_steps)
         same = pedges == edges and all(
             np.array_equal(a, b.cpu().numpy()[:edges]) for a, b in zip(host_edges, (d_rows, d_cols, d_w)))
-        plain = {"ms_per_step": pms, "value": job_cells_per_s(n, ws, pms), "unit": "cells/s", "steps": args.plain_steps,
+        plain = {"ms_per_step": pms, "value": job_cells_per_s(n, 1, pms), "unit": "cells/s", "steps": args.plain_steps,
                  "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in pstats])),
                  "speedup": pms / ms, "identical_edges": bool(same)}
 
@@ -361,7 +392,7 @@ def main():
     stop_only = None
     if learned:
         sms, sstats, _, sedges = timed_device(make_opts("bf16", False), 1, args.steps)
-        stop_only = {"ms_per_step": sms, "value": job_cells_per_s(n, ws, sms), "unit": "cells/s", "steps": args.steps,
+        stop_only = {"ms_per_step": sms, "value": job_cells_per_s(n, 1, sms), "unit": "cells/s", "steps": args.steps,
                      "warmup": 1, "ms_kernel": float(np.mean([s_["ms_kernel"] for s_ in sstats])),
                      "blocks_stopped": sstats[-1]["blocks_stopped"], "same_edge_count": sedges == edges}
         if plain is not None:
@@ -395,14 +426,14 @@ def main():
         traffic = traffic_per_launch(args.backend, pairs, d)
         line = {
             "metric": METRIC,
-            "value": job_cells_per_s(n, ws, ms),
+            "value": job_cells_per_s(n, 1, ms),
             "unit": "cells/s",
             "n_gpus": ws,
             "steps": args.steps,
             "warmup": args.warmup,
             "ms_per_step": ms,
             "higher_is_better": True,
-            "scaling": "weak",
+            "scaling": "strong",
             "vs_baseline": None,
             "dtype": ("split-bf16 tcgen05 tiles (fp32 accumulate) + f64 rescoring" if args.backend == "bf16"
                       else "f32 tiles + f64 rescoring"),
@@ -410,7 +441,7 @@ def main():
             "config": {"workload": wl.name, "n": n, "d": d, "k": k, "margin": wl.margin, "backend": args.backend,
                        "learned_prune": learned, "weight": "tanimoto",
                        "l2": "flushed between steps (512 MB write outside the timed events)"},
-            "e2e": {"value": job_cells_per_s(n, ws, e2e_s * 1e3), "unit": "cells/s", "h2d_bytes_per_step": n * d * 4,
+            "e2e": {"value": job_cells_per_s(n, 1, e2e_s * 1e3), "unit": "cells/s", "h2d_bytes_per_step": n * d * 4 * ws,
                     "d2h_bytes_per_step": edges * 16},
             "gpu_launches": int(launches),
             "gpu_launches_per_step": launches / args.steps,
@@ -419,7 +450,7 @@ def main():
                          "ms_per_launch": kms, "pairs_per_launch": pairs,
                          "executed_tflops": executed / (kms * 1e-3) / 1e12,
                          "executed_frac": executed / (kms * 1e-3) / 1e12 / peak},
-            "pair_dots_per_s": ws * float(n) * (n - 1) / (ms * 1e-3),
+            "pair_dots_per_s": float(n) * (n - 1) / (ms * 1e-3),
             "edges": edges,
             "plain_fp32": plain,
             "without_learned": stop_only,
@@ -431,7 +462,7 @@ def main():
             "clocks": clocks.summary(),
         }
         if train is not None:
-            line["value_incl_training"] = job_cells_per_s(n, ws, ms + train["ms_labels"] + train["ms_train"])
+            line["value_incl_training"] = job_cells_per_s(n, 1, ms + train["ms_labels"] + train["ms_train"])
         if not args.no_cpu:
             v, cores, sample = cpu_baseline(x, wl, target_s=args.cpu_seconds)
             line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample}

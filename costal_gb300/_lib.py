@@ -113,6 +113,8 @@ SIGNATURES = {
     "costal_leiden_many": [U64, P, P, P, U64, P, U64, P, U64, DBL, I32, INT, P, STR, SZ],
     "costal_modularity": [U64, P, P, P, U64, P, DBL, P, STR, SZ],
     "costal_reweight_jaccard_device_noalloc": [P, U64, U32, P, P, STR, SZ],
+    "costal_knn_shard_device": [P, U64, U32, U32, P, U32, U32, P, P, P, P, P, P, P, P, STR, SZ],
+    "costal_fuzzy_union_device": [P, P, U64, U32, P, P, P, P, P, STR, SZ],
     "costal_mlp_train": [P, U64, U32, U32, P, P, STR, SZ],
     "costal_mlp_get": [P, U64, P, P, P, P, STR, SZ],
     "costal_mlp_set": [P, U64, U32, U32, C.c_float, STR, SZ],
@@ -142,6 +144,8 @@ def lib() -> C.CDLL:
         lb.costal_version.restype = C.c_char_p
         lb.costal_launch_count.argtypes = []
         lb.costal_launch_count.restype = C.c_ulonglong
+        lb.costal_shard_rows_max.argtypes = [U64, U32]
+        lb.costal_shard_rows_max.restype = C.c_uint64
         _lib = lb
     return _lib
 

@@ -53,6 +53,7 @@ struct Misc {  // small device-side results read back at the end of a call
     unsigned long long blocks_stopped;
     unsigned long long conv_mismatches;
     unsigned nnz;
+    unsigned shard_rows;  // rows of the shard being computed (the rescoring's device-side row count)
 };
 
 struct Context {
@@ -68,7 +69,7 @@ struct Context {
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
     DevBuf part_idx, part_score, part_tau, tfloor;
-    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm;
+    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm, shard_rows;
     MlpState mlp;
 };
 
@@ -180,10 +181,29 @@ cudaError_t mlp_predict_thresholds(Context& c, prune::Plan& pp, cudaStream_t s) 
     return mlp::block_min(c.mlp_pred.as<float>(), pp.perm, n, pp.tq, s);
 }
 
+// One shard of the query rows (a multi-GPU run gives each rank one): the rows are cut into query
+// blocks of 128 in the order the coarse pass processes them (the input order, or the locality order
+// of the tensor-core path), and shard `index` of `count` takes the contiguous blocks
+// [index·B/count, (index+1)·B/count) of the B blocks. Every column stays in the computation.
+struct Shard {
+    int index = 0, count = 1;
+    int nrows = 0;  // filled: the shard's rows, listed (original ids) in Context::shard_rows
+};
+
+// The query-block range of a shard.
+void shard_blocks(int n, const Shard& sh, int& qb0, int& qb1) {
+    const long long nqb = (n + 127) / 128;
+    qb0 = (int)(nqb * sh.index / sh.count);
+    qb1 = (int)(nqb * (sh.index + 1) / sh.count);
+}
+
 // The kNN on device buffers. Everything is asynchronous on `s` except the final read of Misc.
 // d_w (optional): the Tanimoto weight of every output edge, fused into the rescoring.
+// shard (optional): compute only that shard's rows (their outputs are written at their rows of
+// d_idx/d_cos/d_w; the norms of all rows are written).
 void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn_opts& o, uint32_t* d_idx,
-             double* d_cos, double* d_norms, double* d_w, costal_knn_stats* st, cudaStream_t s) {
+             double* d_cos, double* d_norms, double* d_w, costal_knn_stats* st, cudaStream_t s,
+             Shard* shard = nullptr) {
     const uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
     const int cap = (int)std::min<uint64_t>((uint64_t)k + margin, (uint64_t)n - 1);
     const int dp = coarse_dpad(d);
@@ -191,10 +211,25 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     if (coarse_slots(cap) == 0)
         throw Fail{COSTAL_EUNSUPPORTED, "k + margin = " + std::to_string(k + margin) +
                                             " exceeds the 128 candidates per row the GPU coarse pass keeps"};
+    if (shard && o.select == COSTAL_SELECT_TANIMOTO)
+        throw Fail{COSTAL_EUNSUPPORTED, "row shards support cosine selection only"};
     CK(ensure(c.misc, sizeof(Misc)));
     Misc* dm = c.misc.as<Misc>();
     CK(cudaMemsetAsync(dm, 0, sizeof(Misc), s));
     CK(cudaMemsetAsync(&dm->bad_row, 0xff, 8, s));
+    int qb0 = 0, qb1 = (n + 127) / 128;
+    uint32_t* srows = nullptr;        // the shard's rows (original ids), on the device
+    const unsigned* scount = nullptr;  // their number, on the device
+    if (shard) {
+        shard_blocks(n, *shard, qb0, qb1);
+        shard->nrows = std::max(0, std::min(n, qb1 * 128) - qb0 * 128);
+        CK(ensure(c.shard_rows, (size_t)n * 4));
+        srows = c.shard_rows.as<uint32_t>();
+        c.h_misc->shard_rows = (unsigned)shard->nrows;
+        CK(cudaMemcpyAsync(&dm->shard_rows, &c.h_misc->shard_rows, 4, cudaMemcpyHostToDevice, s));
+        scount = &dm->shard_rows;
+    }
+    const int nrows = shard ? shard->nrows : n;
     CK(ensure(c.xsT, (size_t)dp * np * 4));
     CK(ensure(c.fb_rows, (size_t)n * 4));
     CK(ensure(c.fb_minsim, (size_t)n * 8));
@@ -259,26 +294,36 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                 }
                 CK(prune::build_lists(pp, &dm->blocks_skipped, s));
             }
+            if (shard && nrows > 0) {  // the shard's rows: its query blocks in the processing order
+                if (ordered)
+                    CK(cudaMemcpyAsync(srows, pp.perm + (size_t)qb0 * 128, (size_t)nrows * 4, cudaMemcpyDeviceToDevice,
+                                       s));
+                else
+                    CK(launch_iota(srows, qb0 * 128, nrows, s));
+            }
             CK(cudaEventRecord(c.ev[5], s));
             CK(ensure(c.tc_ws, tc::workspace_bytes(n, d)));
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
             CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan));
             CK(cudaEventRecord(c.ev[6], s));
-            CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr, ordered && o.prune ? pp.list_ub : nullptr,
-                                 ordered ? pp.counts : nullptr, ordered ? pp.ncb : 0, c.cand_idx.as<uint32_t>(),
-                                 c.cand_score.as<float>(), c.tau.as<float>(), &dm->blocks_stopped, &dm->timeout_flag,
-                                 c.sm_count, s));
+            if (nrows > 0)
+                CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr,
+                                     ordered && o.prune ? pp.list_ub : nullptr, ordered ? pp.counts : nullptr,
+                                     ordered ? pp.ncb : 0, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                     c.tau.as<float>(), &dm->blocks_stopped, &dm->timeout_flag, c.sm_count, s, qb0,
+                                     qb1));
             CK(cudaEventRecord(c.ev[2], s));
             // The split-BF16 certificate with its per-row bound (and, with pruning, the skipped
             // blocks' bound); rows that fail it are listed in tc_rows, re-run over ALL columns by the
             // FP32 coarse kernel and rescored with the FP32 bound, whose failures in turn take the
             // full-row regather.
-            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, plan.row_eps, learned ? pp.row_ub : nullptr,
-                              &dm->prune_fail_count, 0.0, cap < n - 1, 0, nullptr, nullptr, d_idx, d_cos, d_w,
-                              c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
-                              dm->max_err_bits, s));
+            if (nrows > 0)
+                CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                  c.tau.as<float>(), d_norms, plan.row_eps, learned ? pp.row_ub : nullptr,
+                                  &dm->prune_fail_count, 0.0, cap < n - 1, 0, srows, scount, d_idx, d_cos, d_w,
+                                  c.tc_rows.as<uint32_t>(), c.fb_minsim.as<double>(), &dm->tc_fail_count,
+                                  dm->max_err_bits, s));
             if (coarse_fp32_smem(dp, cap) > 227 * 1024)
                 throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 re-run of uncertified rows"};
             // How many rows failed decides the re-run's shape (few rows: the columns split across CTAs).
@@ -310,13 +355,21 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         } else {
             if (coarse_fp32_smem(dp, cap) > 227 * 1024)
                 throw Fail{COSTAL_EUNSUPPORTED, "d and k + margin too large for the FP32 coarse kernel"};
-            CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, nullptr, nullptr, c.cand_idx.as<uint32_t>(),
-                                  c.cand_score.as<float>(), c.tau.as<float>(), s));
+            if (!shard) {
+                CK(launch_coarse_fp32(c.xsT.as<float>(), n, np, dp, cap, cap, nullptr, nullptr,
+                                      c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
+            } else if (nrows > 0) {  // the shard's rows, listed, against all columns
+                CK(launch_iota(srows, qb0 * 128, nrows, s));
+                CK(launch_coarse_fp32_split(c.xsT.as<float>(), n, np, dp, cap, cap, srows, scount, nrows, 1, nullptr,
+                                            nullptr, nullptr, nullptr, c.cand_idx.as<uint32_t>(),
+                                            c.cand_score.as<float>(), c.tau.as<float>(), s));
+            }
             CK(cudaEventRecord(c.ev[2], s));
-            CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
-                              c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0, nullptr,
-                              nullptr, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
-                              &dm->fb_count, dm->max_err_bits, s));
+            if (nrows > 0)
+                CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                  c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps, cap < n - 1, 0, srows,
+                                  scount, d_idx, d_cos, d_w, c.fb_rows.as<uint32_t>(), c.fb_minsim.as<double>(),
+                                  &dm->fb_count, dm->max_err_bits, s));
             CK(cudaEventRecord(c.ev[3], s));
         }
         if (cap < n - 1) {
@@ -340,7 +393,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         st->col_block = used_tc ? (uint64_t)tc::BLOCK_N : 128;
         st->blocks_skipped = hm.blocks_skipped;
         st->blocks_stopped = hm.blocks_stopped;
-        st->blocks_total = (uint64_t)((n + 127) / 128) * (uint64_t)((n + st->col_block - 1) / st->col_block);
+        st->blocks_total = (uint64_t)(qb1 - qb0) * (uint64_t)((n + st->col_block - 1) / st->col_block);
         st->margin = margin;
         st->recomputed_rows = used_tc ? hm.tc_fail_count : 0;
         st->pruned_fallback_rows = hm.prune_fail_count;
@@ -677,6 +730,66 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
     });
 }
 
+// ---- row shards (multi-GPU) ------------------------------------------------------------------
+
+uint64_t costal_shard_rows_max(uint64_t n, uint32_t n_shards) {
+    if (n_shards == 0) return 0;
+    const uint64_t nqb = (n + 127) / 128, most = (nqb + n_shards - 1) / n_shards;
+    return std::min<uint64_t>(n, most * 128);
+}
+
+int costal_knn_shard_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                            uint32_t shard, uint32_t n_shards, uint32_t* d_rows, uint64_t* count, uint32_t* d_idx,
+                            double* d_cos, double* d_w, double* d_norms, costal_knn_stats* stats, void* stream,
+                            char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        check_knn_args(n, d, k);
+        if (n_shards == 0 || shard >= n_shards)
+            throw Fail{COSTAL_EINVAL, "shard " + std::to_string(shard) + " of " + std::to_string(n_shards)};
+        const costal_knn_opts o = opts ? *opts : defaults();
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+        const uint64_t nk = n * k;
+        CK(ensure(c.out_idx, nk * 4));
+        CK(ensure(c.out_cos, nk * 8));
+        if (d_w) CK(ensure(c.out_w, nk * 8));
+        Shard sh;
+        sh.index = (int)shard;
+        sh.count = (int)n_shards;
+        run_knn(c, d_x, (int)n, (int)d, (int)k, o, c.out_idx.as<uint32_t>(), c.out_cos.as<double>(), d_norms,
+                d_w ? c.out_w.as<double>() : nullptr, stats, s, &sh);
+        *count = (uint64_t)sh.nrows;
+        if (sh.nrows > 0) {
+            CK(cudaMemcpyAsync(d_rows, c.shard_rows.p, (size_t)sh.nrows * 4, cudaMemcpyDeviceToDevice, s));
+            CK(launch_take_rows(c.shard_rows.as<uint32_t>(), sh.nrows, (int)k, c.out_idx.as<uint32_t>(),
+                                c.out_cos.as<double>(), d_w ? c.out_w.as<double>() : nullptr, d_idx, d_cos, d_w, s));
+        }
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_fuzzy_union_device(const int32_t* d_idx, const double* d_w, uint64_t n, uint32_t k, int32_t* d_rows,
+                              int32_t* d_cols, double* d_wout, uint64_t* m, void* stream, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        *m = 0;
+        const uint64_t nk = n * k;
+        if (nk == 0) return;
+        if (nk > (uint64_t)INT32_MAX) throw Fail{COSTAL_EUNSUPPORTED, "n*k exceeds the int32 range of the GPU path"};
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+        CK(ensure(c.misc, sizeof(Misc)));
+        Misc* dm = c.misc.as<Misc>();
+        CK(cudaMemsetAsync(&dm->first_bad_idx, 0xff, 8, s));
+        CK(launch_check_idx(d_idx, nk, (int)n, &dm->first_bad_idx, s));
+        CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (c.h_misc->first_bad_idx != ~0ull) {  // lib.rs:65-78: report the first bad value
+            int32_t bad = 0;
+            CK(cudaMemcpy(&bad, d_idx + c.h_misc->first_bad_idx, 4, cudaMemcpyDeviceToHost));
+            throw Fail{COSTAL_EINVAL,
+                       "neighbor index " + std::to_string(bad) + " out of range (n=" + std::to_string(n) + ")"};
+        }
+        run_union(c, reinterpret_cast<const uint32_t*>(d_idx), d_w, n, k, d_rows, d_cols, d_wout, m, s);
+    });
+}
 
 // ---- the learned block-pruning model ----------------------------------------------------------
 

@@ -13,6 +13,8 @@
 //                    same sorted, de-duplicated list; (a + b) − a·b is commutative, so which
 //                    direction supplies a never changes a bit (graph.rs:20-23).
 
+#include <algorithm>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,6 +46,29 @@ cudaError_t launch_iota(uint32_t* out, int start, int m, cudaStream_t st) {
     if (m > 0) { k_iota<<<(m + 255) / 256, 256, 0, st>>>(out, start, m); note_launch(); }
     return cudaGetLastError();
 }
+// A shard's outputs packed: packed row r takes row rows[r] of the (n, k) idx / cos / w (w optional).
+// One thread per output entry; rows[] holds valid row ids (the shard's own list).
+__global__ void k_take_rows(const uint32_t* __restrict__ rows, int nrows, int k, const uint32_t* __restrict__ idx,
+                            const double* __restrict__ cos, const double* __restrict__ w, uint32_t* __restrict__ oidx,
+                            double* __restrict__ ocos, double* __restrict__ ow) {
+    const uint64_t total = (uint64_t)nrows * k;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = e / k, t = e - r * k;
+        const uint64_t src = (uint64_t)rows[r] * k + t;
+        oidx[e] = idx[src];
+        ocos[e] = cos[src];
+        if (w) ow[e] = w[src];
+    }
+}
+cudaError_t launch_take_rows(const uint32_t* rows, int nrows, int k, const uint32_t* idx, const double* cos,
+                             const double* w, uint32_t* oidx, double* ocos, double* ow, cudaStream_t st) {
+    const uint64_t total = (uint64_t)nrows * k;
+    if (total == 0) return cudaGetLastError();
+    const unsigned grid = (unsigned)std::min<uint64_t>((total + 255) / 256, 4096);
+    k_take_rows<<<grid, 256, 0, st>>>(rows, nrows, k, idx, cos, w, oidx, ocos, ow); note_launch();
+    return cudaGetLastError();
+}
+
 // Evenly spaced sample rows: out[j] = ⌊j·n/m⌋.
 __global__ void k_stride_rows(uint32_t* __restrict__ out, int m, int n) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;

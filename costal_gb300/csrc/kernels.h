@@ -53,6 +53,9 @@ cudaError_t launch_gather(const float* x, const float* xsT, int n, int np, int d
 
 // ---- graph.cu ----------------------------------------------------------------------------------
 cudaError_t launch_iota(uint32_t* out, int start, int m, cudaStream_t st);
+// Pack the rows `rows[0..nrows)` of (n, k) neighbour arrays into (nrows, k) ones (w may be NULL).
+cudaError_t launch_take_rows(const uint32_t* rows, int nrows, int k, const uint32_t* idx, const double* cos,
+                             const double* w, uint32_t* oidx, double* ocos, double* ow, cudaStream_t st);
 cudaError_t launch_stride_rows(uint32_t* out, int m, int n, cudaStream_t st);
 cudaError_t launch_kth(const double* cos, const uint32_t* rows, int m, int k, float* y, cudaStream_t st);
 cudaError_t launch_init_params(float* P, int F, unsigned long long seed, cudaStream_t st);

@@ -386,7 +386,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const uint32_t* __restrict__ lists, const float* __restrict__ list_ub,
                 const uint32_t* __restrict__ counts, int ncb, const double* __restrict__ row_eps,
                 uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
-                unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag) {
+                unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag,
+                int qb0) {
     constexpr int SL = 2 * SLOTS;  // buffer slots per lane in a flush: BCAP = 2·LCAP entries
     constexpr int BCAP = 32 * SL;
     extern __shared__ unsigned char smem_raw[];
@@ -405,9 +406,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Rows and columns are in the working order (rows sorted by locality cell; perm maps back to the
     // original index). A CTA visits the column blocks of its list, nearest first, or all of them.
-    const int q0 = blockIdx.x * BLOCK_M;
-    const int ntiles = lists ? (int)counts[blockIdx.x] : np / BLOCK_N;
-    const uint32_t* my_list = lists ? lists + (size_t)blockIdx.x * ncb : nullptr;
+    // CTA b takes query block qb0 + b (a launch over a contiguous range of query blocks: one shard).
+    const int qb = qb0 + (int)blockIdx.x;
+    const int q0 = qb * BLOCK_M;
+    const int ntiles = lists ? (int)counts[qb] : np / BLOCK_N;
+    const uint32_t* my_list = lists ? lists + (size_t)qb * ncb : nullptr;
     auto block_of = [&](int t) -> int { return my_list ? (int)my_list[t] : t; };
     const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb_b * B_KB_BYTES;
     (void)a_bytes;
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (warp == EPI_WARPS) {
         // ------------------------------------------------------------------ TMA producer
         if (KLOOP && lane == 0) {
-            const float* my_ub = list_ub ? list_ub + (size_t)blockIdx.x * ncb : nullptr;
+            const float* my_ub = list_ub ? list_ub + (size_t)qb * ncb : nullptr;
             bool go = true;
             for (int t = 0; go && t < ntiles; ++t) {
                 const int cb = block_of(t) * BLOCK_N;
@@ -481,7 +484,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (!KLOOP && lane == 0) {
             mbar_expect_tx(&bars->a_full, a_bytes);
             for (int kb = 0; kb < nkb; ++kb) tma_load_2d(a_tile + kb * A_KB_BYTES, &map_a, kb * KB, q0, &bars->a_full);
-            const float* my_ub = list_ub ? list_ub + (size_t)blockIdx.x * ncb : nullptr;
+            const float* my_ub = list_ub ? list_ub + (size_t)qb * ncb : nullptr;
             for (int t = 0; t < ntiles; ++t) {
                 const int s = t % stages;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u;
@@ -1018,7 +1021,7 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
 cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const float* list_ub,
                           const uint32_t* counts, int ncb, uint32_t* cand_idx, float* cand_score, float* tau,
                           unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
-                          cudaStream_t st) {
+                          cudaStream_t st, int qb0, int qb1) {
     (void)sm_count;
     CUtensorMap ma, mb;
     if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M) || !make_map(&mb, plan.ops_b, plan.kpb, plan.np, BLOCK_N))
@@ -1030,14 +1033,15 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     const size_t smem = fixed + (size_t)stages * per;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
+    if (qb1 < 0) qb1 = qblocks;
+    if (qb0 < 0 || qb1 > qblocks || qb0 >= qb1) return cudaErrorInvalidValue;
     auto kern = !sh.resident ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
                              : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<qblocks, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages, cap,
-                                          plan.perm, lists,
-                                          lists ? list_ub : nullptr, counts, ncb, plan.row_eps, cand_idx, cand_score,
-                                          tau, stopped_total, timeout_flag); note_launch();
+    kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,
+                                            cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, plan.row_eps,
+                                            cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0); note_launch();
     return cudaGetLastError();
 }
 

@@ -30,11 +30,12 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, co
 // All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
 // With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]);
 // with list_ub (their bounds, non-increasing) it stops once no later block can hold an admissible
-// column for any of its rows.
+// column for any of its rows. [qb0, qb1) restricts the launch to those query blocks (one shard of
+// the rows); qb1 = -1 means all of them.
 cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const float* list_ub,
                           const uint32_t* counts, int ncb, uint32_t* cand_idx, float* cand_score, float* tau,
                           unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
-                          cudaStream_t st);
+                          cudaStream_t st, int qb0 = 0, int qb1 = -1);
 
 }  // namespace tc
 }  // namespace costal

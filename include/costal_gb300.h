@@ -126,6 +126,28 @@ int costal_build_graph_device(const float* d_x, uint64_t n, uint32_t d, uint32_t
                               uint32_t weight, int32_t* d_rows, int32_t* d_cols, double* d_w, uint64_t* m,
                               costal_knn_stats* stats, void* stream, char* err, size_t errlen);
 
+/* ---- row shards: the path split across GPUs (knn.rs:403-512 `run_blocked`'s unit of work, a
+ * block of query rows against all columns) -------------------------------------------------------
+ * The query rows are cut into blocks of 128 in the order the coarse pass processes them (the input
+ * order; on the bf16 backend for d <= 64, the locality order, which every rank derives identically
+ * from the same X); shard s of S takes the contiguous blocks [s*B/S, (s+1)*B/S) of the B blocks, so
+ * the S shards hold every row exactly once. Each rank keeps all of X and computes its shard against
+ * every column: the only exchange is gathering the shards' rows afterwards. */
+/* The most rows any of n_shards shards holds (the capacity of the packed outputs). */
+uint64_t costal_shard_rows_max(uint64_t n, uint32_t n_shards);
+/* The kNN of shard `shard` of `n_shards` on device buffers: d_rows receives the shard's rows (original
+ * ids, *count of them), d_idx/d_cos (and d_w, the Tanimoto weight, unless NULL) their neighbours
+ * packed row by row (*count x k); d_norms the norms of all n rows. Cosine selection only. Output
+ * equals the same rows of costal_knn_exact_device. */
+int costal_knn_shard_device(const float* d_x, uint64_t n, uint32_t d, uint32_t k, const costal_knn_opts* opts,
+                            uint32_t shard, uint32_t n_shards, uint32_t* d_rows, uint64_t* count, uint32_t* d_idx,
+                            double* d_cos, double* d_w, double* d_norms, costal_knn_stats* stats, void* stream,
+                            char* err, size_t errlen);
+/* lib.rs:219-239 `_fuzzy_union` on device buffers (the gathered kNN of a sharded run): rows/cols/w_out
+ * hold up to n*k edges; *m is written on the host. */
+int costal_fuzzy_union_device(const int32_t* d_idx, const double* d_w, uint64_t n, uint32_t k, int32_t* d_rows,
+                              int32_t* d_cols, double* d_w_out, uint64_t* m, void* stream, char* err, size_t errlen);
+
 /* Jaccard weights (the computation of costal_reweight with COSTAL_WEIGHT_JACCARD) on DEVICE buffers,
  * for callers that may not allocate device memory: it has no counterpart in the reference. Its scratch is
  * a fixed 16 MiB array compiled into the library (reserved on every GPU that loads it, until the process

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(ext):
     missing = [s for s in declared_symbols() if not hasattr(lib, s)]
     assert not missing, missing
     # every declared entry point has a ctypes signature in the binding
-    bound = set(_lib.SIGNATURES) | {"costal_version", "costal_launch_count"}
+    bound = set(_lib.SIGNATURES) | {"costal_version", "costal_launch_count", "costal_shard_rows_max"}
     assert set(declared_symbols()) <= bound
 
 
