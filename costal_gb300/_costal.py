@@ -14,7 +14,9 @@ Differences from the reference, all documented:
   - `row_block`, `col_block`, `sort_by_norm` and `n_threads` are accepted and validated but do not
     change the GPU tiling (the reference: they change speed only, knn.rs:39-44). `prune` (speed
     only, as in the reference) switches the exact early stop of the bf16 backend's block lists.
-  - k + margin above 128 raises NotImplementedError (the GPU keeps at most 128 candidates a row).
+  - The GPU keeps at most 128 candidates a row: k + margin above 128 runs with margin 128 − k, and
+    k ≥ 128 with the exact f64 scan of every candidate (the output is the same; the margin in effect
+    is reported in the stats).
   - The backend used when a caller passes no `matmul` (as costal.knn and costal.find_communities of the
     reference package never do) is DEFAULT_MATMUL: "fp32" unless the environment variable
     COSTAL_GB300_MATMUL names another backend when this module is imported. Setting it to "bf16" moves

@@ -204,13 +204,31 @@ void shard_blocks(int n, const Shard& sh, int& qb0, int& qb1) {
 void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn_opts& o, uint32_t* d_idx,
              double* d_cos, double* d_norms, double* d_w, costal_knn_stats* st, cudaStream_t s,
              Shard* shard = nullptr) {
-    const uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
-    const int cap = (int)std::min<uint64_t>((uint64_t)k + margin, (uint64_t)n - 1);
+    uint64_t margin = o.margin == UINT32_MAX ? (uint64_t)k : (uint64_t)o.margin;
+    int cap = (int)std::min<uint64_t>((uint64_t)k + margin, (uint64_t)n - 1);
     const int dp = coarse_dpad(d);
     const int np = round_up(n, 128);
-    if (coarse_slots(cap) == 0)
-        throw Fail{COSTAL_EUNSUPPORTED, "k + margin = " + std::to_string(k + margin) +
-                                            " exceeds the 128 candidates per row the GPU coarse pass keeps"};
+    // The coarse passes keep at most 128 candidates a row (fewer for 40 < d ≤ 64, where the query
+    // tile shares the shared memory). The over-selection m changes only how often the certificate
+    // holds, never the output (knn.rs:45-52), so a larger k + m runs with the largest candidate count
+    // the FP32 kernel holds that still exceeds k (rows the certificate then fails take the regather);
+    // when none does, every candidate is scanned exactly in f64 (knn.rs:884-924).
+    bool scan_all = false;
+    auto fits = [&](int c) { return coarse_slots(c) != 0 && coarse_fp32_smem(dp, c) <= 227 * 1024; };
+    if (!fits(cap)) {
+        int smaller = 0;
+        for (int c : {128, 64, 32})
+            if (c < cap && c > k && fits(c)) {
+                smaller = c;
+                break;
+            }
+        if (smaller) {
+            cap = smaller;
+            margin = (uint64_t)(cap - k);
+        } else {
+            scan_all = true;
+        }
+    }
     if (shard && o.select == COSTAL_SELECT_TANIMOTO)
         throw Fail{COSTAL_EUNSUPPORTED, "row shards support cosine selection only"};
     CK(ensure(c.misc, sizeof(Misc)));
@@ -239,13 +257,15 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaEventRecord(c.ev[5], s));
     const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
     bool used_tc = false;
-    if (tanimoto && coarse_fp32_smem(dp, cap) > 227 * 1024) {
-        // (a cap too large for the coarse kernel's shared memory) the exact f64 scan of every
+    if (scan_all) {
+        if (shard) throw Fail{COSTAL_EUNSUPPORTED, "row shards need k + margin within the coarse pass's 128 candidates"};
+        if (gather_smem(k, d, dp) > 227 * 1024) throw Fail{COSTAL_EUNSUPPORTED, "k too large for the GPU scan kernel"};
+        // (no candidate count the coarse kernel holds exceeds k) the exact f64 scan of every
         // candidate on the GPU (knn.rs:884-924's brute force), exact by construction
         CK(cudaEventRecord(c.ev[2], s));
         CK(cudaEventRecord(c.ev[3], s));
-        CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, nullptr, nullptr, nullptr, 1, 1,
-                         std::min(n, 8 * c.sm_count), d_idx, d_cos, d_w, s));
+        CK(launch_gather(d_x, c.xsT.as<float>(), n, np, d, dp, k, d_norms, nullptr, nullptr, nullptr, 1,
+                         tanimoto ? 1 : 0, std::min(n, 8 * c.sm_count), d_idx, d_cos, d_w, s));
     } else if (tanimoto) {
         // Tanimoto selection (knn.rs:197-284): the FP32 pass over all columns with the coarse
         // Tanimoto score, the f64 rescoring of the cap candidates by T with the certificate

@@ -53,12 +53,8 @@ namespace tc {
 constexpr int KB = 64;                 // bf16 elements per 128-byte swizzle row (one K block)
 constexpr int A_KB_BYTES = BLOCK_M * 128;  // 16 KB per K block of the query tile
 constexpr int B_KB_BYTES = BLOCK_N * 128;  // 32 KB per K block of a column tile
-// Eight epilogue warps: warps w and w + 4 read the same 32 TMEM lanes (a warp may only read the lane
-// quarter w mod 4), w the first 128 columns of every tile and w + 4 the last 128, so two warps per
-// scheduler hide each other's fixed-latency chains. They share their 32 queries' buffers.
-constexpr int EPI_WARPS = 8;
-constexpr int NTHREADS = (EPI_WARPS + 2) * 32;  // 8 epilogue warps, 1 TMA warp, 1 MMA warp
-constexpr long long LOCK_LIMIT = 1ll << 22;     // polls of a pair lock before the launch gives up
+constexpr int EPI_WARPS = 4;
+constexpr int NTHREADS = (EPI_WARPS + 2) * 32;  // 4 epilogue warps, 1 TMA warp, 1 MMA warp
 constexpr uint32_t TMEM_COLS = 512;    // two 256-column FP32 accumulators
 constexpr long long WAIT_LIMIT = 1ll << 22;
 
@@ -191,10 +187,7 @@ struct __align__(8) Barriers {
     uint64_t t_empty[2];
     uint32_t tmem_base;
     int stop_tile;         // the list position at which the CTA stops (set by the TMA warp)
-    float warp_floor[EPI_WARPS];  // per epilogue warp: min over its rows of τ − E (never decreases)
-    int lock[4];           // per lane quarter: held by the warp of the pair that is admitting
-    int cnt[BLOCK_M];      // per query: entries in its buffer (read and written under the lock)
-    float tau[BLOCK_M];    // per query: its threshold (written under the lock; only ever rises)
+    float warp_floor[4];   // per epilogue warp: min over its rows of τ − E (never decreases)
 };
 
 // Per-query candidate buffer: BCAP = 2·LCAP entries in shared memory, [entry][query] with a row
@@ -386,49 +379,6 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
     *tau_io = tau;
 }
 
-// The smallest of the epilogue warps' floors (they may be read while being raised: a stale value
-// is lower, which only delays a stop).
-__device__ __forceinline__ float floor_min(const float* wf_) {
-    volatile const float* wf = wf_;
-    float f = wf[0];
-#pragma unroll
-    for (int w = 1; w < EPI_WARPS; ++w) f = fminf(f, wf[w]);
-    return f;
-}
-
-// Admissions of one warp into the buffers its lane quarter shares with the partner warp: under the
-// pair's lock (bounded: on a timeout the launch is flagged and this admission skipped), with the
-// count and threshold of each query read from and written back to shared memory. `tau` is the
-// warp's own copy of its queries' thresholds, raised here to the shared value.
-template <int SL>
-__device__ __forceinline__ void admit_shared(unsigned gmask, uint32_t taddr, int cb, int n, int q, int qi, int qbase,
-                                             int lane, int cap, int q_lo, float* B_s, uint32_t* B_i, Barriers* bars,
-                                             int* lock, float& tau, unsigned long long* timeout_flag) {
-    int ok = 1;
-    if (lane == 0) {
-        long long i = 0;
-        while (atomicCAS(lock, 0, 1) != 0) {
-            if (++i >= LOCK_LIMIT || ((i & 1023) == 0 && *reinterpret_cast<volatile unsigned long long*>(timeout_flag))) {
-                atomicExch(timeout_flag, 1ull);
-                ok = 0;
-                break;
-            }
-        }
-    }
-    ok = __shfl_sync(COSTAL_FULL_MASK, ok, 0);
-    if (!ok) return;
-    __threadfence_block();
-    int cnt = reinterpret_cast<volatile int*>(bars->cnt)[qi];
-    float t = fmaxf(tau, reinterpret_cast<volatile float*>(bars->tau)[qi]);
-    admit_groups<SL>(gmask, taddr, cb, n, q, qi, qbase, lane, cap, q_lo, B_s, B_i, &cnt, &t);
-    reinterpret_cast<volatile int*>(bars->cnt)[qi] = cnt;
-    reinterpret_cast<volatile float*>(bars->tau)[qi] = t;
-    tau = t;
-    __threadfence_block();
-    __syncwarp();
-    if (lane == 0) atomicExch(lock, 0);
-}
-
 template <int SLOTS, bool KLOOP>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
@@ -477,12 +427,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         bars->stop_tile = ntiles;
         for (int w = 0; w < EPI_WARPS; ++w) bars->warp_floor[w] = -CUDART_INF_F;
-        for (int w = 0; w < 4; ++w) bars->lock[w] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    for (int i = threadIdx.x; i < BLOCK_M; i += blockDim.x) {
-        bars->cnt[i] = 0;
-        bars->tau[i] = -CUDART_INF_F;
     }
     if (warp == EPI_WARPS + 1) {  // the MMA warp owns the TMEM allocation
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem_base)),
@@ -515,7 +460,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                             atomicExch(timeout_flag, 2ull);  // never produced by the list kernel
                             stop = true;
                         } else if (t > 0 && my_ub) {
-                            const float fl = floor_min(bars->warp_floor);
+                            volatile float* wf = bars->warp_floor;
+                            const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
                             if (my_ub[t] < fl) {
                                 stop = true;
                                 if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
@@ -556,7 +502,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     // has cosine ≤ my_ub[t]; its coarse score is ≤ my_ub[t] + E_i. When that is below
                     // every row's threshold τ_i, none of them can be admitted: stop here. The floors
                     // read may be stale, i.e. lower, which only delays the stop.
-                    const float fl = floor_min(bars->warp_floor);
+                    volatile float* wf = bars->warp_floor;
+                    const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
                     if (my_ub[t] < fl) {
                         *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
                         if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
@@ -638,21 +585,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
         }
     } else {
-        // ------------------------------------------------------------------ epilogue (warps 0-7)
-        // Warp w reads TMEM lanes 32·(w mod 4) … (its 32 queries) and scans columns [128·⌊w/4⌋, +128)
-        // of every tile; its partner w ± 4 scans the other half. Each keeps its own copy of the
-        // queries' thresholds (it can only be behind the shared one, which admits a little more and
-        // is never wrong: τ only rises) and takes the pair's lock for the rare admissions.
-        const int sub = warp & 3, half = warp >> 2;
-        const int qbase = sub * 32;
+        // ------------------------------------------------------------------ epilogue (warps 0-3)
+        const int qbase = warp * 32;
         const int qi = qbase + lane;  // TMEM lane = query row within the block
         const int q = q0 + qi, q_lo = q0 + qbase;
         // this row's coarse-error bound, rounded up to f32 (rows past n never hold the CTA back)
         const float row_e = q < n ? __double2float_ru(row_eps[perm ? perm[q] : (uint32_t)q]) : 0.0f;
         float tau = -CUDART_INF_F;
+        int cnt = 0;
         const uint32_t lane_addr = tmem + ((uint32_t)qbase << 16);
-        int* lock = &bars->lock[sub];
         uint32_t ra[64], rb[64];
+        int cnt_m = 0;  // cnt and tau round-trip through these when the rare path runs
+        float tau_m = tau;
         for (int t = 0; t < ntiles; ++t) {
             const int buf = t & 1;
             const uint32_t bph = (uint32_t)(t >> 1) & 1u;
@@ -662,10 +606,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int c0 = block_of(t) * BLOCK_N;
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
             if (t == 0) {
-                // A starting threshold from the first tiles (both warps of the pair compute the same):
-                // the cap-th largest of their column-group maxima (64 groups of 8 columns over tiles 0
-                // and 1, 32 over tile 0 alone, or 64 of 4 when cap > 32) is reached by cap distinct
-                // columns, so no other column below it can be among the query's best cap. (When the
+                // A starting threshold from the first tiles: the cap-th largest of their column-group
+                // maxima (64 groups of 8 columns over tiles 0 and 1, 32 over tile 0 alone, or 64 of 4
+                // when cap > 32) is reached by cap distinct columns, so no other column below it can
+                // be among the query's best cap. (When the
                 // query's own column or padding supplies one of those maxima, τ₀ can be a little too
                 // high; that only costs the certificate, since τ never falls and everything left out
                 // stays below it.) The first tile itself is admitted at ≥ τ₀ (one below in the strict
@@ -703,27 +647,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     tau = nextafterf(kth_of<64>(gmax, cap), -CUDART_INF_F);
                 }
             }
-            // This warp's two 64-column slices: the second slice's TMEM load is in flight while the
-            // first is scanned. A slice costs a max tree and a warp OR; only the 8-column groups some
-            // lane needs are re-read and scanned.
-            const uint32_t th = tb + (uint32_t)(128 * half);
-            const int ch = c0 + 128 * half;
-            tmem_ld64(th, ra);
+            // Four 64-column slices, as a two-step software pipeline: the next slice's TMEM load is
+            // in flight while one is scanned. A slice costs a max tree and a warp OR; only the
+            // 8-column groups some lane needs are re-read and scanned.
+            tmem_ld64(tb, ra);
             tmem_wait(ra);
-            tmem_ld64(th + 64, rb);
-            unsigned gm = slice_mask(ra, tau);
-            if (gm) admit_shared<SL>(gm, th, ch, n, q, qi, qbase, lane, cap, q_lo, B_s, B_i, bars, lock, tau, timeout_flag);
-            tmem_wait(rb);
-            gm = slice_mask(rb, tau);
-            if (gm)
-                admit_shared<SL>(gm, th + 64, ch + 64, n, q, qi, qbase, lane, cap, q_lo, B_s, B_i, bars, lock, tau,
-                                 timeout_flag);
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                tmem_ld64(tb + (uint32_t)(128 * h + 64), rb);
+                unsigned gm = slice_mask(ra, tau);
+                if (gm) {
+                    cnt_m = cnt;
+                    tau_m = tau;
+                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h), c0 + 128 * h, n, q, qi, qbase, lane, cap, q_lo, B_s,
+                                     B_i, &cnt_m, &tau_m);
+                    cnt = cnt_m;
+                    tau = tau_m;
+                }
+                tmem_wait(rb);
+                if (h == 0) tmem_ld64(tb + 128, ra);
+                gm = slice_mask(rb, tau);
+                if (gm) {
+                    cnt_m = cnt;
+                    tau_m = tau;
+                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h + 64), c0 + 128 * h + 64, n, q, qi, qbase, lane, cap,
+                                     q_lo, B_s, B_i, &cnt_m, &tau_m);
+                    cnt = cnt_m;
+                    tau = tau_m;
+                }
+                if (h == 0) tmem_wait(ra);
+            }
             // every TMEM read of this accumulator is complete: hand it back to the MMA warp
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bars->t_empty[buf]);
-            // the partner's admissions may have raised the shared threshold
-            tau = fmaxf(tau, reinterpret_cast<volatile float*>(bars->tau)[qi]);
             // the warp's floor min(τ − E) for the TMA warp's stop test (signed-int order of the f32)
             if (list_ub) {
                 const float f = q < n ? __fsub_rd(tau, row_e) : CUDART_INF_F;
@@ -734,25 +691,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         __int_as_float(key >= 0 ? key : key ^ 0x7fffffff);
             }
         }
-        // both warps of the pair are done with the buffers (a named barrier of the pair's 64 threads);
-        // then the first selects every buffer down to its best `cap` entries (in buffer order)
-        __threadfence_block();
-        asm volatile("bar.sync %0, 64;" ::"r"(1 + sub) : "memory");
-        if (half == 0) {
-            int cnt = reinterpret_cast<volatile int*>(bars->cnt)[qi];
-            tau = fmaxf(tau, reinterpret_cast<volatile float*>(bars->tau)[qi]);
-            flush_full<SL>(B_s, B_i, qbase, lane, cap, cap, cnt, tau);
-            __syncwarp();
-            if (q < n) {
-                const uint32_t qo = perm ? perm[q] : (uint32_t)q;
-                for (int p = 0; p < cap; ++p) {
-                    // an empty slot (fewer than cap candidates) carries index 0xffffffff and score −inf
-                    const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0xffffffffu;
-                    cand_idx[(size_t)qo * cap + p] = cw < (uint32_t)n ? (perm ? perm[cw] : cw) : 0xffffffffu;
-                    cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
-                }
-                tau_out[qo] = tau;
+        // final selection: every buffer down to its best `cap` entries (in buffer order)
+        flush_full<SL>(B_s, B_i, qbase, lane, cap, cap, cnt, tau);
+        __syncwarp();
+        if (q < n) {
+            const uint32_t qo = perm ? perm[q] : (uint32_t)q;
+            for (int p = 0; p < cap; ++p) {
+                // an empty slot (fewer than cap candidates) carries index 0xffffffff and score −inf
+                const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0xffffffffu;
+                cand_idx[(size_t)qo * cap + p] = cw < (uint32_t)n ? (perm ? perm[cw] : cw) : 0xffffffffu;
+                cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
             }
+            tau_out[qo] = tau;
         }
     }
     tc_fence_before();

@@ -267,9 +267,18 @@ __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const
 // ---- per-query-block lists ------------------------------------------------------------------------
 
 constexpr int LIST_T = 512;
-constexpr int LIST_KPT = 16;                 // list entries per thread
-constexpr int LIST_N = LIST_T * LIST_KPT;    // 8192: the most column blocks a list is sorted for
 constexpr double XI = 1e-6;
+
+// A list sort's shape: KPT keys per thread over LIST_T threads (16 → 8,192 column blocks, two CTAs
+// per SM; 32 → 16,384, one CTA per SM with the keys in its registers). The low key word packs the
+// centre angle above the complemented block id: ID_BITS bits of id, 32 − ID_BITS of angle.
+template <int KPT>
+struct ListShape {
+    static constexpr int N = LIST_T * KPT;
+    static constexpr int ID_BITS = KPT <= 16 ? 13 : 14;
+    static constexpr uint32_t ID_MAX = (1u << ID_BITS) - 1u;
+    static constexpr uint32_t PHI_MAX = (1u << (32 - ID_BITS)) - 1u;
+};
 
 // The bound in f32 for one (query block, column block) pair, rigorous for the f64 geometry: the
 // f32 FMA dot of the two unit centres (each rounded to f32) is within (d + 2)·2⁻²⁴ of the f64 value,
@@ -349,15 +358,16 @@ __device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk
     }
 }
 
-// The sorted keys out: list position e holds block 8191 − (low 13 bits) and its bound.
-template <int KPT>
+// The sorted keys out: list position e holds block ID_MAX − (low ID_BITS bits) and its bound.
+template <int KPT, int ID_BITS>
 __device__ __forceinline__ void write_keys(const uint64_t (&v)[KPT], int base, unsigned nk, uint32_t* out, float* out_ub) {
+    constexpr uint32_t ID_MAX = (1u << ID_BITS) - 1u;
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         const unsigned e = (unsigned)(base + j);
         if (e < nk) {
             const uint32_t hk = (uint32_t)(v[j] >> 32);
-            out[e] = 8191u - ((uint32_t)v[j] & 8191u);
+            out[e] = ID_MAX - ((uint32_t)v[j] & ID_MAX);
             out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
         }
     }
@@ -365,13 +375,13 @@ __device__ __forceinline__ void write_keys(const uint64_t (&v)[KPT], int base, u
 
 // Compact the kept keys (non-zero) of every thread into xk[0 .. kept) in any order, zero-fill up to
 // LIST_T·KPT, and load KPT of them per thread.
-template <int KPT>
-__device__ __forceinline__ void compact_keys(const uint64_t (&all)[LIST_KPT], uint64_t (&v)[KPT], uint64_t* xk,
+template <int KPT, int KPT_ALL>
+__device__ __forceinline__ void compact_keys(const uint64_t (&all)[KPT_ALL], uint64_t (&v)[KPT], uint64_t* xk,
                                              unsigned* slot, unsigned nk, int base) {
     constexpr int N = LIST_T * KPT;
     for (int e = threadIdx.x + (int)nk; e < N; e += LIST_T) xk[e] = 0ull;
 #pragma unroll
-    for (int j = 0; j < LIST_KPT; ++j)
+    for (int j = 0; j < KPT_ALL; ++j)
         if (all[j]) xk[atomicAdd(slot, 1u)] = all[j];
     __syncthreads();
 #pragma unroll
@@ -382,14 +392,16 @@ __device__ __forceinline__ void compact_keys(const uint64_t (&all)[LIST_KPT], ui
 // One CTA per query block: the upper bound against every column block; the blocks kept (UB ≥ t_Q)
 // sorted by (UB desc, centre angle asc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
 // exchanged in registers, by warp shuffles or through shared memory by distance — and the largest UB
-// of a skipped block. Lists longer than LIST_N stay in block order with bounds +inf.
-__global__ void __launch_bounds__(LIST_T, 2)
+// of a skipped block. Lists longer than the shape's N stay in block order with bounds +inf.
+template <int KPT_ALL>
+__global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
                   const float* __restrict__ ccenter_f, const float* __restrict__ cradius_f, int nqb, int ncb, int d,
                   const float* __restrict__ tq, uint32_t* __restrict__ lists, float* __restrict__ list_ub,
                   uint32_t* __restrict__ counts, float* __restrict__ ub_skip,
                   unsigned long long* __restrict__ skipped_total) {
-    extern __shared__ uint64_t xk[];  // [LIST_N] exchange buffer
+    using LS = ListShape<KPT_ALL>;
+    extern __shared__ uint64_t xk[];  // [LS::N] exchange buffer
     __shared__ float cq[64];
     __shared__ unsigned kept, slot;
     __shared__ int skip_max_bits;
@@ -406,7 +418,7 @@ __global__ void __launch_bounds__(LIST_T, 2)
     const float t = tq ? tq[Q] : -CUDART_INF_F;
     uint32_t* out = lists + (size_t)Q * ncb;
     float* out_ub = list_ub + (size_t)Q * ncb;
-    if (ncb > LIST_N) {
+    if (ncb > LS::N) {
         if (tid == 0) {
             unsigned c = 0;
             for (int b = 0; b < ncb; ++b) {
@@ -421,14 +433,14 @@ __global__ void __launch_bounds__(LIST_T, 2)
             kept = c;
         }
     } else {
-        const int base = tid * LIST_KPT;
-        uint64_t v[LIST_KPT];
+        const int base = tid * KPT_ALL;
+        uint64_t v[KPT_ALL];
         unsigned my_kept = 0;
         int my_skip = __float_as_int(-CUDART_INF_F);
         // keys are computed for blocks j·LIST_T + tid (coalesced reads of the transposed centres); the
         // sort does not care where each key starts
 #pragma unroll
-        for (int j = 0; j < LIST_KPT; ++j) {
+        for (int j = 0; j < KPT_ALL; ++j) {
             const int b = j * LIST_T + tid;
             v[j] = 0ull;  // absent or skipped: sorts last
             if (b < ncb) {
@@ -440,9 +452,10 @@ __global__ void __launch_bounds__(LIST_T, 2)
                     const uint32_t ub = __float_as_uint(u);
                     const uint32_t hk = (ub & 0x80000000u) ? ~ub : (ub | 0x80000000u);
                     // ties of the bound (e.g. every block of the query's own cluster at 1) go nearest
-                    // centre first, then by block: the low word is (2^19 − 1 − φ quantised) · 2^13 + (8191 − b)
-                    const uint32_t qphi = (uint32_t)fminf(524287.0f, fmaxf(0.0f, phi) * (524288.0f / 3.14159265f));
-                    const uint32_t lo = ((524287u - qphi) << 13) | (8191u - (uint32_t)b);
+                    // centre first, then by block: the low word is (PHI_MAX − φ quantised) · 2^ID_BITS + (ID_MAX − b)
+                    const uint32_t qphi = (uint32_t)fminf((float)LS::PHI_MAX,
+                                                          fmaxf(0.0f, phi) * ((float)(LS::PHI_MAX + 1u) / 3.14159265f));
+                    const uint32_t lo = ((LS::PHI_MAX - qphi) << LS::ID_BITS) | (LS::ID_MAX - (uint32_t)b);
                     v[j] = ((uint64_t)hk << 32) | (uint64_t)lo;
                 } else {
                     // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
@@ -455,20 +468,26 @@ __global__ void __launch_bounds__(LIST_T, 2)
         __syncthreads();  // kept is final
         const unsigned nk = kept;
         // Short lists (a learned threshold skips most blocks) sort only their kept keys, compacted.
+        constexpr int IB = LS::ID_BITS;
         if (nk <= (unsigned)(LIST_T * 4)) {
             uint64_t w[4];
             compact_keys<4>(v, w, xk, &slot, nk, tid * 4);
             block_sort_keys<4>(w, xk, tid * 4, lane);
-            write_keys<4>(w, tid * 4, nk, out, out_ub);
+            write_keys<4, IB>(w, tid * 4, nk, out, out_ub);
         } else if (nk <= (unsigned)(LIST_T * 8)) {
             uint64_t w[8];
             compact_keys<8>(v, w, xk, &slot, nk, tid * 8);
             block_sort_keys<8>(w, xk, tid * 8, lane);
-            write_keys<8>(w, tid * 8, nk, out, out_ub);
+            write_keys<8, IB>(w, tid * 8, nk, out, out_ub);
+        } else if (KPT_ALL > 16 && nk <= (unsigned)(LIST_T * 16)) {
+            uint64_t w[16];
+            compact_keys<16>(v, w, xk, &slot, nk, tid * 16);
+            block_sort_keys<16>(w, xk, tid * 16, lane);
+            write_keys<16, IB>(w, tid * 16, nk, out, out_ub);
         } else {
-            // the keys start interleaved over all LIST_N positions, so the sort covers all of them
-            block_sort_keys<LIST_KPT>(v, xk, base, lane);
-            write_keys<LIST_KPT>(v, base, nk, out, out_ub);
+            // the keys start interleaved over all N positions, so the sort covers all of them
+            block_sort_keys<KPT_ALL>(v, xk, base, lane);
+            write_keys<KPT_ALL, IB>(v, base, nk, out, out_ub);
         }
     }
     __syncthreads();
@@ -593,11 +612,15 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
 }
 
 cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t st) {
-    const size_t smem = (size_t)LIST_N * 8;
-    cudaError_t e = cudaFuncSetAttribute(k_block_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // up to 8,192 column blocks (n ≤ 2,097,152): 16 keys a thread, two CTAs per SM; up to 16,384
+    // (n ≤ 4,194,304): 32 keys a thread; beyond that the lists stay in block order (no early stop)
+    const bool wide = P.ncb > ListShape<16>::N;
+    auto kern = wide ? k_block_lists<32> : k_block_lists<16>;
+    const size_t smem = (size_t)(wide ? ListShape<32>::N : ListShape<16>::N) * 8;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_block_lists<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq,
-                                              P.lists, P.list_ub, P.counts, P.ub_skip, skipped_total); note_launch();
+    kern<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq, P.lists,
+                                      P.list_ub, P.counts, P.ub_skip, skipped_total); note_launch();
     k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub); note_launch();
     return cudaGetLastError();
 }

@@ -490,3 +490,16 @@ def test_certificate_bound_holds_on_adversarial_rows(ext, oracle, kind, d):
         print(f"{kind} d={d} {backend}: max |coarse - exact| {st['max_coarse_err']:.3g}, "
               f"max ratio to the bound {st['max_err_ratio']:.3g}, recomputed {st['recomputed_rows']}")
         assert st["max_err_ratio"] < 1.0, st
+
+
+@pytest.mark.parametrize("n,d,k,margin", [(5000, 16, 100, None), (3000, 60, 40, 40), (1500, 8, 150, None),
+                                          (1200, 24, 300, 5)])
+@pytest.mark.parametrize("backend", ["fp32", "bf16"])
+def test_large_k_and_margin(ext, oracle, n, d, k, margin, backend):
+    """knn.rs:449 accepts any 1 <= k <= n-1 with cap = min(k + m, n - 1): beyond the candidates the
+    GPU coarse pass holds, the margin in effect shrinks (the output is the same) and for k >= 128 every
+    candidate is scanned in f64; the answer equals the oracle's brute force bit for bit."""
+    x = clustered(n, d, 40 + d)
+    (idx, cos, norms), st = ext._knn_exact(x, k, margin=margin, matmul=backend)
+    same(as_oracle((idx, cos, norms)), oracle.knn_bruteforce(x, k))
+    assert st["margin"] <= (k if margin is None else margin)

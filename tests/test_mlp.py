@@ -108,3 +108,22 @@ def test_constant_threshold_ablation_and_checkpoint_round_trip(ext, zipf_case):
     print("visited blocks: trained", _visited(st_mlp), "constant", _visited(st_c))
     _, st_back = ext._knn_exact(x, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
     assert st_back["blocks_skipped"] == st_mlp["blocks_skipped"]
+
+
+def test_model_trained_on_one_draw_prunes_another(ext, zipf_case):
+    """Training amortises: the model trained on one draw of the 2,000,000 x 40 generator (here its
+    60,000-row form, seed 4) is applied unchanged to another draw (seed 5). The answer is exact, the
+    threshold still skips blocks up front, and its skips hold for nearly every row (a row whose skip
+    is not certified is rescanned, so the answer never depends on the model)."""
+    from costal_gb300 import workloads as W
+
+    _, wl, _, _ = zipf_case
+    x2 = W.zipf_2m(n=60_000, seed=5)
+    want = ext._knn_exact(x2, wl.k, margin=wl.margin)[0]
+    got, st = ext._knn_exact(x2, wl.k, margin=wl.margin, matmul="bf16", learned_prune=True)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+    assert st["blocks_skipped"] > 0.04 * st["blocks_total"], st
+    assert st["pruned_fallback_rows"] < 0.01 * len(x2), st
+    print("other draw: learned skips", st["blocks_skipped"], "of", st["blocks_total"], "rescanned rows",
+          st["pruned_fallback_rows"])
