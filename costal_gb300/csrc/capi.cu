@@ -69,7 +69,7 @@ struct Context {
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
     DevBuf part_idx, part_score, part_tau, tfloor;
-    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm, shard_rows;
+    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm, shard_rows, tani_perm, tani_ws;
     MlpState mlp;
 };
 
@@ -275,8 +275,18 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         CK(ensure(c.tau, (size_t)n * 4));
         CK(ensure(c.tnorm, (size_t)n * 8));
         const double eps_t = 2.0 * ((double)d + 12.0) * F32_EPS;
-        CK(launch_coarse_fp32_tanimoto(c.xsT.as<float>(), n, np, dp, cap, d_norms, c.tnorm.as<float2>(),
-                                       c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
+        if (o.prune && cap < n - 1 && dp <= 64) {
+            // the norm window (knn.rs:595-644): rows in norm order, each query block walking outward
+            CK(ensure(c.tani_perm, (size_t)n * 4));
+            CK(ensure(c.tani_ws, std::max(prune::norm_order_bytes(n), tani_window_bytes(n, np, dp))));
+            CK(prune::norm_order(d_norms, n, c.tani_ws.p, c.tani_perm.as<uint32_t>(), s));
+            CK(launch_coarse_tani_window(c.xsT.as<float>(), n, np, dp, cap, d_norms, c.tani_perm.as<uint32_t>(),
+                                         c.tani_ws.p, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                         c.tau.as<float>(), &dm->blocks_skipped, s));
+        } else {
+            CK(launch_coarse_fp32_tanimoto(c.xsT.as<float>(), n, np, dp, cap, d_norms, c.tnorm.as<float2>(),
+                                           c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(), c.tau.as<float>(), s));
+        }
         CK(cudaEventRecord(c.ev[2], s));
         CK(launch_rescore(d_x, n, d, k, cap, cap, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
                           c.tau.as<float>(), d_norms, nullptr, nullptr, nullptr, eps_t, cap < n - 1, 1, nullptr,

@@ -182,6 +182,58 @@ __device__ __forceinline__ void tani_tile(float (&acc)[8][8], const float2* __re
     }
 }
 
+// The 8 × 8 register tile of one 128 × 128 tile: the FMA chains over the depth in dimension order
+// (queries ty·4+i and 64+ty·4+i of A_s, columns tx·4+j and 64+tx·4+j of the stage Bst).
+template <int DPC>
+__device__ __forceinline__ void tile_fma(const float* A_s, const float* Bst, int dp, int tx, int ty, float (&acc)[8][8]) {
+#if COSTAL_FP32_PAIRED
+    // Blackwell's paired FP32 FMA: one instruction does two independent single-rounding FMAs,
+    // so the values are those of the scalar fmaf chain below.
+    unsigned long long acc2[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
+#pragma unroll(DPC ? DPC : 4)
+    for (int t = 0; t < dp; ++t) {
+        const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
+        const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const unsigned long long bp[4] = {pack2(b0.x, b0.y), pack2(b0.z, b0.w), pack2(b1.x, b1.y), pack2(b1.z, b1.w)};
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const unsigned long long ap = pack2(a[i], a[i]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc2[i][j] = ffma2(ap, bp[j], acc2[i][j]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
+#else
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+#pragma unroll(DPC ? DPC : 4)
+    for (int t = 0; t < dp; ++t) {
+        const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
+        const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+#endif
+}
+
 template <int SLOTS, int DPC, bool TANI>
 __global__ void __launch_bounds__(NT, 1)
     k_coarse_fp32(const float* __restrict__ xsT, int n, int np, int dp_rt, int cap, int lstride,
@@ -254,52 +306,7 @@ __global__ void __launch_bounds__(NT, 1)
         const int c0 = (tile0 + tl) * BN;
 
         float acc[8][8];
-#if COSTAL_FP32_PAIRED
-        // Blackwell's paired FP32 FMA: one instruction does two independent single-rounding FMAs,
-        // so the values are those of the scalar fmaf chain below.
-        unsigned long long acc2[8][4];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc2[i][j] = 0ull;
-#pragma unroll(DPC ? DPC : 4)
-        for (int t = 0; t < dp; ++t) {
-            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
-            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
-            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
-            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const unsigned long long bp[4] = {pack2(b0.x, b0.y), pack2(b0.z, b0.w), pack2(b1.x, b1.y), pack2(b1.z, b1.w)};
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const unsigned long long ap = pack2(a[i], a[i]);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc2[i][j] = ffma2(ap, bp[j], acc2[i][j]);
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) unpack2(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
-#else
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
-#pragma unroll(DPC ? DPC : 4)
-        for (int t = 0; t < dp; ++t) {
-            const float4 a0 = *reinterpret_cast<const float4*>(A_s + t * BM + ty * 4);
-            const float4 a1 = *reinterpret_cast<const float4*>(A_s + t * BM + 64 + ty * 4);
-            const float4 b0 = *reinterpret_cast<const float4*>(Bst + t * BN + tx * 4);
-            const float4 b1 = *reinterpret_cast<const float4*>(Bst + t * BN + 64 + tx * 4);
-            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-#endif
+        tile_fma<DPC>(A_s, Bst, dp, tx, ty, acc);
         if constexpr (TANI) {
             int rows8[8];  // this thread's 8 query rows (their norms enter the Tanimoto scores)
 #pragma unroll
@@ -326,6 +333,228 @@ __global__ void __launch_bounds__(NT, 1)
     cp_async_wait<0>();
     __syncthreads();
     write_lists(L_s, L_i, tau_s, LCAP, cap, lstride, n, nq, q0, part_stride, row_of, cand_idx, cand_score, tau_out);
+}
+
+// Tanimoto selection with the norm window (knn.rs:197-284 `Tanimoto`, :595-644 `coarse_block`):
+// the rows in norm order (the working order W; perm maps back), each CTA's 128 query rows scan the
+// column tile of their own norms first and then walk outward, right (larger norms) and left
+// (smaller), one tile each way in turn. With c = τ/(1+τ), a column of norm b can reach a row's
+// threshold τ > 0 only if ρ = b/a lies in [ρ−, ρ+], the roots of ρ + 1/ρ = q with
+// q = (1+τ)/τ·(1 + 1e-4) (knn.rs:270-283; cos ≤ 1); a side stops at the first tile whose norms all
+// lie outside every row's window (every later tile of that side lies further out, and the windows
+// only shrink as τ rises). A column left out this way has exact T < τ, so the certificate
+// s_k > τ + E that the rescoring checks still covers it. Columns are not visited in index order,
+// so ties at τ may be broken differently than in the unpruned pass; the certificate (or the
+// regather) makes the answer the same.
+template <int SLOTS>
+__global__ void __launch_bounds__(NT, 1)
+    k_coarse_tani_window(const float* __restrict__ xsW, int n, int np, int dp, int cap, const float2* __restrict__ tnW,
+                         const double* __restrict__ normW, const double* __restrict__ tile_lo,
+                         const double* __restrict__ tile_hi, const uint32_t* __restrict__ perm,
+                         uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
+                         unsigned long long* __restrict__ skipped_total) {
+    constexpr int LCAP = 32 * SLOTS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* A_s = reinterpret_cast<float*>(smem_raw);            // [dp][BM]
+    float* B_s = A_s + (size_t)dp * BM;                          // [STAGES][dp][BN]
+    float* L_s = B_s + (size_t)STAGES * dp * BN;                 // [BM][LCAP]
+    uint32_t* L_i = reinterpret_cast<uint32_t*>(L_s + BM * LCAP);
+    float* buf_s = reinterpret_cast<float*>(L_i + BM * LCAP);   // [BM][BUF]
+    uint32_t* buf_i = reinterpret_cast<uint32_t*>(buf_s + BM * BUF);
+    int* cnt_s = reinterpret_cast<int*>(buf_i + BM * BUF);       // [BM]
+    int* len_s = cnt_s + BM;                                     // [BM]
+    float* tau_s = reinterpret_cast<float*>(len_s + BM);         // [BM]
+    float* floor_s = tau_s + BM;                                 // [BM]
+    __shared__ double win_lo_w[4], win_hi_w[4];
+    __shared__ int win_ok_w[4];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int q0 = blockIdx.x * BM;  // working rows q0 .. q0 + 127
+    auto row_of = [&](int qi) -> int { return q0 + qi; };
+    const int all_tiles = np / BN;
+    const int mid = min(all_tiles - 1, (q0 + BM / 2) / BN);  // the tile of the block's own norms
+    auto load_tile = [&](float* dst, int c0) {
+        for (int ch = tid; ch < dp * (BN / 4); ch += NT) {
+            const int t = ch / (BN / 4), c4 = ch % (BN / 4);
+            cp_async16(dst + t * BN + c4 * 4, xsW + (size_t)t * np + c0 + c4 * 4);
+        }
+    };
+    // The visiting order, the same in every thread: mid, then right and left in turn; a stopped
+    // side yields no more tiles.
+    int right = mid + 1, left = mid - 1;
+    bool rstop = false, lstop = false, take_right = true;
+    auto next_tile = [&]() -> int {
+        for (int tries = 0; tries < 2; ++tries) {
+            const bool r = take_right;
+            take_right = !take_right;
+            if (r && !rstop && right < all_tiles) return right++;
+            if (!r && !lstop && left >= 0) return left--;
+        }
+        return -1;
+    };
+    int stage_tile[STAGES];
+    load_tile(A_s, q0);
+    stage_tile[0] = mid;
+    load_tile(B_s, mid * BN);
+    cp_async_commit();
+    stage_tile[1] = next_tile();
+    if (stage_tile[1] >= 0) load_tile(B_s + (size_t)dp * BN, stage_tile[1] * BN);
+    cp_async_commit();
+    for (int q = tid; q < BM; q += NT) {
+        cnt_s[q] = 0;
+        len_s[q] = 0;
+        floor_s[q] = -CUDART_INF_F;
+        tau_s[q] = -CUDART_INF_F;
+    }
+    for (int e = tid; e < BM * LCAP; e += NT) {
+        L_s[e] = -CUDART_INF_F;
+        L_i[e] = 0xffffffffu;
+    }
+    bool win_ok = false;  // every row's window is defined (its list is full and τ > 0)
+    double win_lo = 0.0, win_hi = 0.0;
+    int scanned = 0;
+    for (int it = 0;; ++it) {
+        const int s = it % STAGES;
+        const int tile = stage_tile[s];
+        if (tile < 0) break;
+        cp_async_wait<1>();
+        __syncthreads();  // the stage landed for every thread; stage (it+2)%3 is free again
+        const int nxt = next_tile();
+        stage_tile[(it + 2) % STAGES] = nxt;
+        if (nxt >= 0) load_tile(B_s + (size_t)((it + 2) % STAGES) * dp * BN, nxt * BN);
+        cp_async_commit();
+        if (tile != mid && win_ok) {
+            // a side ends at its first tile outside every row's window (knn.rs:617-639)
+            if (tile > mid && tile_lo[tile] > win_hi) {
+                rstop = true;
+                continue;
+            }
+            if (tile < mid && tile_hi[tile] < win_lo) {
+                lstop = true;
+                continue;
+            }
+        }
+        ++scanned;
+        const float* Bst = B_s + (size_t)s * dp * BN;
+        const int c0 = tile * BN;
+        float acc[8][8];
+        tile_fma<0>(A_s, Bst, dp, tx, ty, acc);
+        int rows8[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int r = row_of(i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+            rows8[i] = r < n ? r : -1;
+        }
+        tani_tile(acc, tnW, c0, n, tx, ty, rows8);
+        select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
+                           row_of, [&](int qi, int cl) {
+                               float sv = 0.0f;
+                               for (int t = 0; t < dp; ++t) sv = fmaf(A_s[t * BM + qi], Bst[t * BN + cl], sv);
+                               const int q = row_of(qi), col = c0 + cl;
+                               return tani_coarse_f32(sv, q < n ? tnW[q] : make_float2(0.0f, 0.0f),
+                                                      col < n ? tnW[col] : make_float2(0.0f, 0.0f));
+                           });
+        __syncthreads();  // every query's τ after this tile
+        // The union of the rows' windows in absolute norms (knn.rs:668-678), in f64.
+        if (tid < BM) {
+            const int w = q0 + tid;
+            double lo = CUDART_INF, hi = -CUDART_INF;
+            int ok = 1;
+            if (w < n) {
+                const float tf = tau_s[tid];
+                if (!(tf > 0.0f)) {
+                    ok = 0;
+                } else {
+                    const double tau = (double)tf;
+                    const double q = (1.0 + tau) / tau * (1.0 + 1e-4);
+                    const double disc = sqrt(fmax(q * q - 4.0, 0.0));
+                    const double a = normW[w];
+                    lo = (q - disc) / 2.0 * a;
+                    hi = (q + disc) / 2.0 * a;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fmin(lo, __shfl_xor_sync(COSTAL_FULL_MASK, lo, o));
+                hi = fmax(hi, __shfl_xor_sync(COSTAL_FULL_MASK, hi, o));
+                ok &= __shfl_xor_sync(COSTAL_FULL_MASK, ok, o);
+            }
+            if (lane == 0) {
+                win_lo_w[warp] = lo;
+                win_hi_w[warp] = hi;
+                win_ok_w[warp] = ok;
+            }
+        }
+        __syncthreads();
+        win_ok = win_ok_w[0] && win_ok_w[1] && win_ok_w[2] && win_ok_w[3];
+        win_lo = fmin(fmin(win_lo_w[0], win_lo_w[1]), fmin(win_lo_w[2], win_lo_w[3]));
+        win_hi = fmax(fmax(win_hi_w[0], win_hi_w[1]), fmax(win_hi_w[2], win_hi_w[3]));
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    // the lists out, in the input order: rows and columns mapped back through perm
+    for (int e = tid; e < BM * cap; e += NT) {
+        const int qi = e / cap, p = e % cap, w = q0 + qi;
+        if (w >= n) continue;
+        const uint32_t c = L_i[qi * LCAP + p];
+        const size_t o = (size_t)perm[w] * cap + p;
+        cand_idx[o] = c < (uint32_t)n ? perm[c] : 0xffffffffu;
+        cand_score[o] = L_s[qi * LCAP + p];
+    }
+    for (int qi = tid; qi < BM; qi += NT)
+        if (q0 + qi < n) tau_out[perm[q0 + qi]] = tau_s[qi];
+    if (tid == 0 && skipped_total) atomicAdd(skipped_total, (unsigned long long)(all_tiles - scanned));
+}
+
+// The norm-ordered working copy for the windowed pass: xsW[t][w] = xsT[t][perm[w]] (zero for w ≥ n),
+// the rows' f32 norm and squared norm, their f64 norms, and each 128-column tile's norm range.
+__global__ void k_tani_gather(const float* __restrict__ xsT, int n, int np, int dp, const uint32_t* __restrict__ perm,
+                              float* __restrict__ xsW) {
+    const size_t total = (size_t)dp * np;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int t = (int)(e / np), w = (int)(e % np);
+        xsW[e] = w < n ? xsT[(size_t)t * np + perm[w]] : 0.0f;
+    }
+}
+__global__ void k_tani_norms_w(const double* __restrict__ norms, int n, const uint32_t* __restrict__ perm,
+                               float2* __restrict__ tnW, double* __restrict__ normW) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n) return;
+    const double a = norms[perm[w]];
+    tnW[w] = make_float2((float)a, (float)(a * a));  // knn.rs:207-212 rounds ‖x‖² to f32
+    normW[w] = a;
+}
+__global__ void k_tile_norm_range(const double* __restrict__ normW, int n, int ntiles, double* __restrict__ lo,
+                                  double* __restrict__ hi) {
+    const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (tile >= ntiles) return;
+    double a = CUDART_INF, b = -CUDART_INF;
+    for (int j = lane; j < BN; j += 32) {
+        const int w = tile * BN + j;
+        if (w < n) {
+            a = fmin(a, normW[w]);
+            b = fmax(b, normW[w]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_xor_sync(COSTAL_FULL_MASK, a, o));
+        b = fmax(b, __shfl_xor_sync(COSTAL_FULL_MASK, b, o));
+    }
+    if (lane == 0) {
+        lo[tile] = a;  // a tile of padding only: +inf / −inf, outside every window
+        hi[tile] = b;
+    }
+}
+// The ranges made monotone along the order (rows inside a norm bucket are not sorted, so a later
+// tile may hold a smaller norm than an earlier one): lo[t] = the smallest norm of tiles t, t+1, …
+// and hi[t] = the largest of tiles …, t−1, t. A side stopped at tile t then has every later tile of
+// that side outside the window too. (One thread: a few thousand tiles.)
+__global__ void k_tile_norm_envelope(int ntiles, double* __restrict__ lo, double* __restrict__ hi) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int t = ntiles - 2; t >= 0; --t) lo[t] = fmin(lo[t], lo[t + 1]);
+    for (int t = 1; t < ntiles; ++t) hi[t] = fmax(hi[t], hi[t - 1]);
 }
 
 // The same pass for any depth: the dimensions stream through the 3-stage ring in chunks of KC rows
@@ -633,6 +862,49 @@ cudaError_t launch_coarse_fp32_tanimoto(const float* xsT, int n, int np, int dp,
     k_tani_norms<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, st>>>(norms, n, tnorm); note_launch();
     return plain::launch_any(xsT, n, np, dp, cap, cap, nullptr, nullptr, 1, 0, 0, nullptr, tnorm, cand_idx, cand_score,
                              tau, st);
+}
+
+namespace {
+inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+}  // namespace
+
+size_t tani_window_bytes(int n, int np, int dp) {
+    const size_t ntiles = (size_t)np / plain::BN;
+    return al256((size_t)dp * np * 4) + al256((size_t)n * 8) * 2 + al256(ntiles * 8) * 2 + 256;
+}
+
+cudaError_t launch_coarse_tani_window(const float* xsT, int n, int np, int dp, int cap, const double* norms,
+                                      const uint32_t* perm, void* ws, uint32_t* cand_idx, float* cand_score,
+                                      float* tau, unsigned long long* skipped_total, cudaStream_t st) {
+    using namespace plain;
+    if (dp > 64) return cudaErrorInvalidValue;
+    const int ntiles = np / BN;
+    char* p = static_cast<char*>(ws);
+    float* xsW = reinterpret_cast<float*>(p);
+    p += al256((size_t)dp * np * 4);
+    float2* tnW = reinterpret_cast<float2*>(p);
+    p += al256((size_t)n * 8);
+    double* normW = reinterpret_cast<double*>(p);
+    p += al256((size_t)n * 8);
+    double* lo = reinterpret_cast<double*>(p);
+    p += al256((size_t)ntiles * 8);
+    double* hi = reinterpret_cast<double*>(p);
+    const size_t total = (size_t)dp * np;
+    k_tani_gather<<<(unsigned)std::min<size_t>((total + 255) / 256, 8192), 256, 0, st>>>(xsT, n, np, dp, perm, xsW);
+    note_launch();
+    k_tani_norms_w<<<(n + 255) / 256, 256, 0, st>>>(norms, n, perm, tnW, normW); note_launch();
+    k_tile_norm_range<<<(ntiles + 7) / 8, 256, 0, st>>>(normW, n, ntiles, lo, hi); note_launch();
+    k_tile_norm_envelope<<<1, 32, 0, st>>>(ntiles, lo, hi); note_launch();
+    const int slots = coarse_slots(cap);
+    const size_t smem = coarse_smem_bytes(dp, slots);
+    auto kern = slots == 1 ? k_coarse_tani_window<1> : (slots == 2 ? k_coarse_tani_window<2> : k_coarse_tani_window<4>);
+    if (slots == 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<np / BM, NT, smem, st>>>(xsW, n, np, dp, cap, tnW, normW, lo, hi, perm, cand_idx, cand_score, tau,
+                                    skipped_total);
+    note_launch();
+    return cudaGetLastError();
 }
 
 int coarse_fp32_segments(int count, int np, int sm_count) {

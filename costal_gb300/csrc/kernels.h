@@ -33,6 +33,14 @@ cudaError_t launch_coarse_fp32_split(const float* xsT, int n, int np, int dp, in
 cudaError_t launch_coarse_fp32_tanimoto(const float* xsT, int n, int np, int dp, int cap, const double* norms,
                                         float2* tnorm, uint32_t* cand_idx, float* cand_score, float* tau,
                                         cudaStream_t st);
+// Tanimoto selection with the norm window (knn.rs:595-644): rows in the norm order `perm` (working →
+// original, prune::norm_order), each query block walking outward from its own norms and stopping a
+// side once its norms leave every row's window; d_pad ≤ 64. ws holds tani_window_bytes(n, np, dp)
+// (the norm-ordered working copy, norms and tile ranges); the lists are written in input order.
+size_t tani_window_bytes(int n, int np, int dp);
+cudaError_t launch_coarse_tani_window(const float* xsT, int n, int np, int dp, int cap, const double* norms,
+                                      const uint32_t* perm, void* ws, uint32_t* cand_idx, float* cand_score,
+                                      float* tau, unsigned long long* skipped_total, cudaStream_t st);
 // The floor of rows re-run after the tensor-core pass (rows[0..*count), cand_* and tau of that pass).
 cudaError_t launch_rerun_floor(const uint32_t* rows, const unsigned* count, int nmax, int cap, const float* tau,
                                const float* cand_score, const double* row_eps, double eps, float* tfloor,

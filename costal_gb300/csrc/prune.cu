@@ -611,6 +611,70 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     return cudaGetLastError();
 }
 
+// The smallest and largest positive norm (order-preserving u64 bits of positive doubles).
+__global__ void k_norm_range(const double* __restrict__ norms, int n, unsigned long long* __restrict__ range) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = norms[i];
+        if (a > 0.0) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+            lo = min(lo, b);
+            hi = max(hi, b);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(COSTAL_FULL_MASK, lo, o));
+        hi = max(hi, __shfl_xor_sync(COSTAL_FULL_MASK, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&range[0], lo);
+        atomicMax(&range[1], hi);
+    }
+}
+
+// Bucket of every row: 0 for a zero row, else 1 + ⌊(NORM_BUCKETS − 2)·log(a/lo)/log(hi/lo)⌋.
+__global__ void k_norm_bucket(const double* __restrict__ norms, int n, const unsigned long long* __restrict__ range,
+                              uint32_t* __restrict__ cell) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = norms[i];
+    const double lo = __longlong_as_double((long long)range[0]), hi = __longlong_as_double((long long)range[1]);
+    uint32_t b = 0;
+    if (a > 0.0) {
+        const double span = hi > lo ? log(hi / lo) : 1.0;
+        const double f = log(a / lo) / span * (double)(NORM_BUCKETS - 2);
+        b = 1u + (uint32_t)fmin(fmax(f, 0.0), (double)(NORM_BUCKETS - 2));
+    }
+    cell[i] = b;
+}
+
+size_t norm_order_bytes(int n) {
+    const size_t nch = (size_t)(n + CHUNK - 1) / CHUNK;
+    return a256((size_t)n * 4) + a256(nch * NORM_BUCKETS * 4) + a256((NORM_BUCKETS + 1) * 4) + 256;
+}
+
+cudaError_t norm_order(const double* norms, int n, void* ws, uint32_t* perm, cudaStream_t st) {
+    char* p = static_cast<char*>(ws);
+    const int nch = (n + CHUNK - 1) / CHUNK;
+    uint32_t* cell = reinterpret_cast<uint32_t*>(p);
+    p += a256((size_t)n * 4);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(p);
+    p += a256((size_t)nch * NORM_BUCKETS * 4);
+    uint32_t* start = reinterpret_cast<uint32_t*>(p);
+    p += a256((NORM_BUCKETS + 1) * 4);
+    unsigned long long* range = reinterpret_cast<unsigned long long*>(p);
+    cudaError_t e = cudaMemsetAsync(range, 0xff, 8, st);  // smallest: all ones
+    if (e == cudaSuccess) e = cudaMemsetAsync(range + 1, 0, 8, st);  // largest: zero
+    if (e != cudaSuccess) return e;
+    k_norm_range<<<std::min((n + 255) / 256, 1024), 256, 0, st>>>(norms, n, range); note_launch();
+    k_norm_bucket<<<(n + 255) / 256, 256, 0, st>>>(norms, n, range, cell); note_launch();
+    k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(cell, n, NORM_BUCKETS, hist); note_launch();
+    k_cell_scan<<<1, NORM_BUCKETS, 0, st>>>(hist, nch, NORM_BUCKETS, start); note_launch();
+    k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(cell, n, NORM_BUCKETS, hist, perm); note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t st) {
     // up to 8,192 column blocks (n ≤ 2,097,152): 16 keys a thread, two CTAs per SM; up to 16,384
     // (n ≤ 4,194,304): 32 keys a thread; beyond that the lists stay in block order (no early stop)

@@ -41,5 +41,13 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
 // Per-query-block column lists with the thresholds in plan.tq (NULL: keep all, nearest first).
 cudaError_t build_lists(Plan& plan, unsigned long long* skipped_total, cudaStream_t st);
 
+// Rows grouped by norm for Tanimoto selection's norm window (knn.rs:413-418 sorts by norm): a stable
+// counting sort into NORM_BUCKETS buckets spaced evenly in log(norm) between the smallest and the
+// largest positive norm (zero rows first). Within a bucket rows keep their input order; the window
+// test only needs each column tile's exact norm range, so the order inside a bucket does not matter.
+constexpr int NORM_BUCKETS = 1024;
+size_t norm_order_bytes(int n);
+cudaError_t norm_order(const double* norms, int n, void* ws, uint32_t* perm, cudaStream_t st);
+
 }  // namespace prune
 }  // namespace costal

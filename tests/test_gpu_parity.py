@@ -503,3 +503,30 @@ def test_large_k_and_margin(ext, oracle, n, d, k, margin, backend):
     (idx, cos, norms), st = ext._knn_exact(x, k, margin=margin, matmul=backend)
     same(as_oracle((idx, cos, norms)), oracle.knn_bruteforce(x, k))
     assert st["margin"] <= (k if margin is None else margin)
+
+
+@pytest.mark.parametrize("n,d,k,spread,signed", [(20_000, 12, 10, 8.0, False), (6000, 40, 15, 3.0, False),
+                                                 (5000, 16, 10, 4.0, True), (3000, 64, 30, 6.0, False)])
+def test_tanimoto_norm_window(ext, oracle, n, d, k, spread, signed):
+    """knn.rs:595-644 on the GPU: with pruning on, each query block walks outward through the norm
+    order and stops a side at the first tile outside every row's norm window. The answer equals the
+    oracle's (and the pass without the window); on positive rows of widely spread norms tiles are
+    skipped, and none with prune=False. Signed rows can have thresholds <= 0, where no window exists."""
+    rng = np.random.default_rng(n + d)
+    means = rng.normal(0, 2, size=(10, d))
+    x = means[rng.integers(0, 10, n)] + rng.normal(0, 0.6, size=(n, d))
+    if not signed:
+        x = np.abs(x)
+    x = x * np.exp(rng.uniform(0, np.log(spread), size=(n, 1)))
+    x[:3] = 0.0  # zero rows: Tanimoto 0 with every row
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    want = oracle.knn_bruteforce(x, k, select="tanimoto")
+    got, st = ext._knn_exact(x, k, select="tanimoto")
+    same(as_oracle(got), want)
+    got0, st0 = ext._knn_exact(x, k, select="tanimoto", prune=False)
+    same(as_oracle(got0), want)
+    assert st0["blocks_skipped"] == 0
+    print(f"n={n} d={d} spread={spread} signed={signed}: window skipped {st['blocks_skipped']} of "
+          f"{st['blocks_total']} tiles, regathered {st['fallback_rows']}")
+    if not signed and spread >= 6.0:
+        assert st["blocks_skipped"] > 0.2 * st["blocks_total"], st
