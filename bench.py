@@ -211,7 +211,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="zipf_2m")
     ap.add_argument("--n", type=int, default=None, help="a smaller n from the same generator (profiling)")
-    ap.add_argument("--backend", default="bf16", choices=["fp32", "bf16"])
+    ap.add_argument("--backend", default="bf16", choices=["fp32", "bf16", "bf16x3", "fp8"],
+                    help="bf16: tensor cores (split BF16; split FP8 for d >= 512); bf16x3 / fp8: that kind only")
     ap.add_argument("--no-learned", action="store_true", help="bf16 backend without the learned pruning")
     ap.add_argument("--train-sample", type=int, default=200_000)
     ap.add_argument("--train-epochs", type=int, default=60)
@@ -245,14 +246,15 @@ def main():
 
     lib = L.lib()
     n, d, k = wl.n, wl.d, wl.k
-    learned = args.backend == "bf16" and not args.no_learned
+    learned = args.backend != "fp32" and not args.no_learned and wl.d <= 64
     err, errlen = L.errbuf()
 
     def make_opts(backend, learned_prune):
         o = L.KnnOpts()
         o.margin = wl.margin
         o.select = 0
-        o.backend = L.BACKEND_BF16 if backend == "bf16" else L.BACKEND_FP32
+        o.backend = {"fp32": L.BACKEND_FP32, "bf16": L.BACKEND_BF16, "bf16x3": L.BACKEND_BF16X3,
+                     "fp8": L.BACKEND_FP8}[backend]
         o.sort_by_norm = 1
         o.prune = 1
         o.learned_prune = 1 if learned_prune else 0
@@ -290,7 +292,7 @@ def main():
         from costal_gb300 import shard as S
 
         (r, c, w), _, stt = S.build_graph_sharded(
-            xd, k, margin=wl.margin, matmul="bf16" if o.backend == L.BACKEND_BF16 else "fp32",
+            xd, k, margin=wl.margin, matmul=args.backend if o.backend != L.BACKEND_FP32 else "fp32",
             learned_prune=bool(o.learned_prune))
         shard_stats.update(stt)
         m.value = r.shape[0]
@@ -381,7 +383,7 @@ def main():
 
     # ---- the plain FP32 GPU path on the same input (the comparison the metric names)
     plain = None
-    if args.backend == "bf16" and args.plain_steps > 0:
+    if args.backend != "fp32" and args.plain_steps > 0:
         pms, pstats, _, pedges = timed_device(make_opts("fp32", False), 1, args.plain_steps)
         same = pedges == edges and all(
             np.array_equal(a, b.cpu().numpy()[:edges]) for a, b in zip(host_edges, (d_rows, d_cols, d_w)))
@@ -420,11 +422,21 @@ def main():
         s0 = stats[-1]
         kms = float(np.mean([s_["ms_kernel"] for s_ in stats]))
         total_blocks = s0["blocks_total"]
-        skipped = s0["blocks_skipped"] + s0["blocks_stopped"] if args.backend == "bf16" else 0
+        tensor = args.backend != "fp32"
+        skipped = s0["blocks_skipped"] + s0["blocks_stopped"] if tensor else 0
         visited = 1.0 - skipped / total_blocks if total_blocks else 1.0
         pairs = float(n) * float(n) * visited  # dense pairs of the visited (query block, column block) tiles
         flops = 2.0 * d * pairs
-        if args.backend == "bf16":
+        kind = s0.get("coarse_kind", 1 if tensor else 0)
+        if tensor and kind == 2:
+            # split FP8: e4m3 MMAs, K = 3d padded to 128; the dense FP8 rate is twice the BF16 one
+            kpad = (3 * d + 127) // 128 * 128
+            tiles = (total_blocks - skipped)
+            executed = 2.0 * kpad * tiles * 128 * 256
+            bound, peak, unit = "tensor", 2.0 * pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s"
+            kernel = "k_coarse_tc (split-FP8 e4m3 tcgen05 tiles + top-(k+m) selection)"
+            peak_kind = f"fp8 dense = 2 x bf16 dense sustained ({pk_kind}; no fp8 figure is measured)"
+        elif tensor:
             kpad = (3 * d + 63) // 64 * 64
             tiles = (total_blocks - skipped)
             executed = 2.0 * kpad * tiles * 128 * 256
@@ -440,7 +452,7 @@ def main():
             kernel = "k_coarse_fp32 (FP32 tiles + top-(k+m) selection)"
             peak_kind = "derived FP32-FFMA peak at max SM clock"
         achieved = flops / (kms * 1e-3) / 1e12
-        traffic = traffic_per_launch(args.backend, pairs, d)
+        traffic = traffic_per_launch("bf16" if kind else "fp32", pairs, d) if kind != 2 else None
         line = {
             "metric": METRIC,
             "value": job_cells_per_s(n, 1, ms),
@@ -452,8 +464,8 @@ def main():
             "higher_is_better": True,
             "scaling": "strong",
             "vs_baseline": None,
-            "dtype": ("split-bf16 tcgen05 tiles (fp32 accumulate) + f64 rescoring" if args.backend == "bf16"
-                      else "f32 tiles + f64 rescoring"),
+            "dtype": ({0: "f32 tiles", 1: "split-bf16 tcgen05 tiles (fp32 accumulate)",
+                       2: "split-fp8 e4m3 tcgen05 tiles (fp32 accumulate)"}[kind] + " + f64 rescoring"),
             "data": "synthetic (seeded generator with the workload's shapes and distributions)",
             "config": {"workload": wl.name, "n": n, "d": d, "k": k, "margin": wl.margin, "backend": args.backend,
                        "learned_prune": learned, "weight": "tanimoto",

@@ -8,9 +8,10 @@ libcostal_gb300.so: the kNN graph on the GPU, Leiden (the host consumer) in host
 
 Differences from the reference, all documented:
   - `matmul` names a coarse-pass backend of this library: "fp32" (default; "gemm" is accepted as
-    its alias) or "bf16" (certified split-BF16 tcgen05 tiles). Like the reference's backends they
-    change speed only, never the output. "accelerate" is Apple-only and unavailable here, as it is
-    for the reference on Linux.
+    its alias), "bf16" (certified tcgen05 tiles: split BF16, or split FP8 e4m3 for d >= 512),
+    "bf16x3" (split BF16 at every depth) or "fp8" (split FP8 wherever the query tile is streamed,
+    3d > 128). Like the reference's backends they change speed only, never the output.
+    "accelerate" is Apple-only and unavailable here, as it is for the reference on Linux.
   - `row_block`, `col_block`, `sort_by_norm` and `n_threads` are accepted and validated but do not
     change the GPU tiling (the reference: they change speed only, knn.rs:39-44). `prune` (speed
     only, as in the reference) switches the exact early stop of the bf16 backend's block lists.
@@ -79,7 +80,8 @@ def row_l2_norms(x):
 
 
 _SELECT_NAMES = ("cosine", "tanimoto")
-_BACKENDS = {"fp32": L.BACKEND_FP32, "gemm": L.BACKEND_FP32, "bf16": L.BACKEND_BF16}
+_BACKENDS = {"fp32": L.BACKEND_FP32, "gemm": L.BACKEND_FP32, "bf16": L.BACKEND_BF16, "bf16x3": L.BACKEND_BF16X3,
+             "fp8": L.BACKEND_FP8}
 
 DEFAULT_MATMUL = os.environ.get("COSTAL_GB300_MATMUL", "fp32")
 if DEFAULT_MATMUL not in _BACKENDS:
@@ -159,6 +161,7 @@ def _knn_exact(x, k, *, select=None, margin=None, row_block=None, col_block=None
         "pruned_fallback_rows": int(st.pruned_fallback_rows),
         "max_coarse_err": float(st.max_coarse_err),
         "max_err_ratio": float(st.max_err_ratio),
+        "coarse_kind": L.COARSE_KINDS[int(st.coarse_kind)],
         "blocks_stopped": int(st.blocks_stopped),
         "ms_order": float(st.ms_order),
         "ms_coarse": float(st.ms_coarse),

@@ -21,6 +21,9 @@ COSTAL_EUNSUPPORTED = 6
 
 BACKEND_FP32 = 0
 BACKEND_BF16 = 1
+BACKEND_BF16X3 = 2
+BACKEND_FP8 = 3
+COARSE_KINDS = ("fp32", "bf16", "fp8")
 SELECT = {"cosine": 0, "tanimoto": 1}
 WEIGHT = {"tanimoto": 0, "cosine": 1, "jaccard": 2}
 
@@ -58,6 +61,7 @@ class KnnStats(C.Structure):
         ("ms_kernel", C.c_double),
         ("blocks_stopped", C.c_uint64),
         ("max_err_ratio", C.c_double),
+        ("coarse_kind", C.c_uint64),
     ]
 
     def as_dict(self):

@@ -257,6 +257,21 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaEventRecord(c.ev[5], s));
     const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
     bool used_tc = false;
+    // The split-FP8 kind: its coarse scores are ~2⁻⁸ coarser than split BF16's, so it keeps 64
+    // candidates a row whatever the margin (the output does not depend on it) to let the certificate
+    // hold for nearly every row.
+    const bool tc_backend = o.backend == COSTAL_BACKEND_BF16 || o.backend == COSTAL_BACKEND_BF16X3 ||
+                            o.backend == COSTAL_BACKEND_FP8;
+    bool fp8 = !tanimoto && !scan_all && (o.backend == COSTAL_BACKEND_FP8 || (o.backend == COSTAL_BACKEND_BF16 && d >= 512));
+    if (fp8) {
+        const int cap8 = std::max(cap, std::min(64, n - 1));
+        if (tc::supported_fp8(d, cap8) && coarse_slots(cap8) != 0 && coarse_fp32_smem(dp, cap8) <= 227 * 1024) {
+            cap = cap8;
+            margin = (uint64_t)(cap - k);
+        } else {
+            fp8 = false;
+        }
+    }
     if (scan_all) {
         if (shard) throw Fail{COSTAL_EUNSUPPORTED, "row shards need k + margin within the coarse pass's 128 candidates"};
         if (gather_smem(k, d, dp) > 227 * 1024) throw Fail{COSTAL_EUNSUPPORTED, "k too large for the GPU scan kernel"};
@@ -305,7 +320,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         CK(ensure(c.cand_score, (size_t)n * cap * 4));
         CK(ensure(c.tau, (size_t)n * 4));
         const double eps = ((double)d + 4.0) * F32_EPS;  // knn.rs:185-187
-        if (o.backend == COSTAL_BACKEND_BF16 && tc::supported(d, cap)) {
+        if (tc_backend && (fp8 || tc::supported(d, cap))) {
             used_tc = true;
             // Locality order (k-means cells) and per-query-block column lists, nearest blocks first;
             // with a learned threshold, blocks whose bound is below it are skipped. Deep rows (the
@@ -332,10 +347,10 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                     CK(launch_iota(srows, qb0 * 128, nrows, s));
             }
             CK(cudaEventRecord(c.ev[5], s));
-            CK(ensure(c.tc_ws, tc::workspace_bytes(n, d)));
+            CK(ensure(c.tc_ws, tc::workspace_bytes(n, d, fp8)));
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
-            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan));
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan, fp8));
             CK(cudaEventRecord(c.ev[6], s));
             if (nrows > 0)
                 CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr,
@@ -432,6 +447,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
         st->max_coarse_err = me;
         std::memcpy(&me, &hm.max_err_bits[1], 8);
         st->max_err_ratio = me;
+        st->coarse_kind = used_tc ? (fp8 ? 2 : 1) : 0;
         st->ms_prep = elapsed(c.ev[0], c.ev[1]);
         st->ms_order = elapsed(c.ev[1], c.ev[5]);
         st->ms_coarse = elapsed(c.ev[5], c.ev[2]);

@@ -38,6 +38,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
@@ -124,6 +125,24 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
         : "memory");
+}
+// kind::f8f6f4 with both operands e4m3 (format code 0) and an F32 accumulator: 32 elements (bytes)
+// of K per instruction, so the shared-memory descriptors advance by the same 32 bytes per step.
+constexpr uint32_t IDESC_E4M3 = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BLOCK_N >> 3) << 17) |
+                                ((uint32_t)(BLOCK_M >> 4) << 24);
+__device__ __forceinline__ void mma_e4m3(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(IDESC_E4M3), "r"(accumulate)
+        : "memory");
+}
+template <bool FP8>
+__device__ __forceinline__ void mma_kind(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    if constexpr (FP8)
+        mma_e4m3(tmem_d, adesc, bdesc, accumulate);
+    else
+        mma_bf16(tmem_d, adesc, bdesc, accumulate);
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -379,7 +398,7 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
     *tau_io = tau;
 }
 
-template <int SLOTS, bool KLOOP>
+template <int SLOTS, bool KLOOP, bool FP8 = false>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
                 int nkb, int nkb_b, int ksteps, int k1s, int stages, int cap, const uint32_t* __restrict__ perm,
@@ -389,6 +408,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag,
                 int qb0) {
     constexpr int SL = 2 * SLOTS;  // buffer slots per lane in a flush: BCAP = 2·LCAP entries
+    // The split-FP8 kind computes on the rows scaled by 2^8, so its accumulators hold 2^16 × the
+    // coarse score: thresholds and admissions stay in those units, the lists and floors are scaled
+    // back exactly.
+    constexpr float OSCALE = FP8 ? 0x1p-16f : 1.0f;
+    constexpr int KBE = FP8 ? 128 : KB;  // elements in one 128-byte K block (the TMA x coordinate step)
     constexpr int BCAP = 32 * SL;
     extern __shared__ unsigned char smem_raw[];
     // 1024-byte alignment for the swizzled tiles
@@ -476,14 +500,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                     mbar_expect_tx(&bars->b_full[s], (uint32_t)(A_KB_BYTES + B_KB_BYTES));
                     unsigned char* dst = b_tiles + (size_t)s * stage_bytes;
-                    tma_load_2d(dst, &map_a, kb * KB, q0, &bars->b_full[s]);
-                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
+                    tma_load_2d(dst, &map_a, kb * KBE, q0, &bars->b_full[s]);
+                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KBE, cb, &bars->b_full[s]);
                 }
             }
         }
         if (!KLOOP && lane == 0) {
             mbar_expect_tx(&bars->a_full, a_bytes);
-            for (int kb = 0; kb < nkb; ++kb) tma_load_2d(a_tile + kb * A_KB_BYTES, &map_a, kb * KB, q0, &bars->a_full);
+            for (int kb = 0; kb < nkb; ++kb) tma_load_2d(a_tile + kb * A_KB_BYTES, &map_a, kb * KBE, q0, &bars->a_full);
             const float* my_ub = list_ub ? list_ub + (size_t)qb * ncb : nullptr;
             for (int t = 0; t < ntiles; ++t) {
                 const int s = t % stages;
@@ -517,7 +541,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 // (the last K block may reach past the operand's row: TMA fills those columns with zeros
                 // and reads nothing for them)
                 for (int kb = 0; kb < nkb_b; ++kb)
-                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KB, cb, &bars->b_full[s]);
+                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KBE, cb, &bars->b_full[s]);
             }
         }
     } else if (warp == EPI_WARPS + 1) {
@@ -547,7 +571,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const int nks = min(4, ksteps - 4 * kb);
                     for (int ks = 0; ks < nks; ++ks) {
                         const uint32_t koff = (uint32_t)(ks * 32);  // 16 bf16 = 32 bytes inside the swizzle row
-                        mma_bf16(d, sw128_desc(a_base + koff), sw128_desc(b_base + koff), (kb | ks) ? 1u : 0u);
+                        mma_kind<FP8>(d, sw128_desc(a_base + koff), sw128_desc(b_base + koff), (kb | ks) ? 1u : 0u);
                     }
                     mma_commit(&bars->b_empty[s]);
                 }
@@ -578,7 +602,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const int kb = ks < k1s ? ks : ks - k1s;
                     const uint64_t ad = sw128_desc(a_base + (uint32_t)(ks >> 2) * A_KB_BYTES + (uint32_t)((ks & 3) * 32));
                     const uint64_t bd = sw128_desc(b_base + (uint32_t)(kb >> 2) * B_KB_BYTES + (uint32_t)((kb & 3) * 32));
-                    mma_bf16(d, ad, bd, ks > 0 ? 1u : 0u);
+                    mma_kind<FP8>(d, ad, bd, ks > 0 ? 1u : 0u);
                 }
                 mma_commit(&bars->b_empty[s]);
                 mma_commit(&bars->t_full[buf]);
@@ -683,7 +707,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (lane == 0) mbar_arrive(&bars->t_empty[buf]);
             // the warp's floor min(τ − E) for the TMA warp's stop test (signed-int order of the f32)
             if (list_ub) {
-                const float f = q < n ? __fsub_rd(tau, row_e) : CUDART_INF_F;
+                const float f = q < n ? __fsub_rd(tau * OSCALE, row_e) : CUDART_INF_F;
                 int key = __float_as_int(f);
                 key = __reduce_min_sync(COSTAL_FULL_MASK, key >= 0 ? key : key ^ 0x7fffffff);
                 if (lane == 0)
@@ -700,9 +724,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 // an empty slot (fewer than cap candidates) carries index 0xffffffff and score −inf
                 const uint32_t cw = p < cnt ? B_i[p * BSTRIDE + qi] : 0xffffffffu;
                 cand_idx[(size_t)qo * cap + p] = cw < (uint32_t)n ? (perm ? perm[cw] : cw) : 0xffffffffu;
-                cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] : -CUDART_INF_F;
+                cand_score[(size_t)qo * cap + p] = p < cnt ? B_s[p * BSTRIDE + qi] * OSCALE : -CUDART_INF_F;
             }
-            tau_out[qo] = tau;
+            tau_out[qo] = tau * OSCALE;
         }
     }
     tc_fence_before();
@@ -853,6 +877,75 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// e4m3 bits → value (exact): sign, 4-bit exponent biased by 7, 3-bit significand; exponent 0 is
+// subnormal (m · 2⁻⁹). 0x7f / 0xff (NaN) never occur: the inputs are finite and well inside ±448.
+__device__ __forceinline__ float e4m3_value(uint8_t b) {
+    const int e = (b >> 3) & 15, m = b & 7;
+    const float mag = e ? ldexpf((float)(8 + m), e - 10) : ldexpf((float)m, -9);
+    return (b & 0x80) ? -mag : mag;
+}
+
+// The split-FP8 operands: a row a (normalised f32) becomes u = 2⁸·a (exact; |u| ≤ 256 < 448, so
+// e4m3's normal range covers every entry above 2⁻¹⁴) split into e4m3 pieces u = hi + lo + r', written
+// as A = [hi | lo | hi], B = [hi | hi | lo] (bytes, zero-padded to kp), one CTA per working row. The
+// piece norms are those of the unscaled pieces h = hi/2⁸, l = lo/2⁸, r = a − h − l (each difference
+// exact in f32: the pieces round to nearest, so each is within a factor two of what it approximates),
+// so the certificate bound of k_row_eps applies unchanged.
+constexpr float FP8_SCALE = 256.0f;
+__global__ void __launch_bounds__(256)
+    k_split_wide_fp8(const float* __restrict__ xsT, int n, int np_x, int d, int kp, const uint32_t* __restrict__ perm,
+                     uint8_t* __restrict__ opa, uint8_t* __restrict__ opb, double* __restrict__ pnorm,
+                     unsigned long long* __restrict__ colmax) {
+    __shared__ double red[4][256];
+    const int r = blockIdx.x, tid = threadIdx.x;
+    const bool live = r < n;
+    const int o = live ? (perm ? (int)perm[r] : r) : 0;
+    uint8_t* ra = opa + (size_t)r * kp;
+    uint8_t* rb = opb + (size_t)r * kp;
+    double sh = 0.0, sl = 0.0, sr = 0.0, sp = 0.0;
+    for (int t = tid; t < d; t += 256) {
+        const float a = live ? xsT[(size_t)t * np_x + o] : 0.0f;
+        const uint8_t hb = (uint8_t)__nv_cvt_float_to_fp8(a * FP8_SCALE, __NV_SATFINITE, __NV_E4M3);
+        const float h = e4m3_value(hb) * (1.0f / FP8_SCALE);
+        const float e = a - h;  // exact in f32
+        const uint8_t lb = (uint8_t)__nv_cvt_float_to_fp8(e * FP8_SCALE, __NV_SATFINITE, __NV_E4M3);
+        const float l = e4m3_value(lb) * (1.0f / FP8_SCALE);
+        const float rem = e - l;  // exact in f32
+        ra[t] = hb;
+        ra[d + t] = lb;
+        ra[2 * d + t] = hb;
+        rb[t] = hb;
+        rb[d + t] = hb;
+        rb[2 * d + t] = lb;
+        const double h64 = f64_of(h), l64 = f64_of(l), r64 = f64_of(rem);  // exact widenings
+        sh = __fma_rn(h64, h64, sh);
+        sl = __fma_rn(l64, l64, sl);
+        sr = __fma_rn(r64, r64, sr);
+        const double p = h64 + l64;
+        sp = __fma_rn(p, p, sp);
+    }
+    for (int t = 3 * d + tid; t < kp; t += 256) {
+        ra[t] = 0;
+        rb[t] = 0;
+    }
+    red[0][tid] = sh;
+    red[1][tid] = sl;
+    red[2][tid] = sr;
+    red[3][tid] = sp;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (tid < h)
+            for (int j = 0; j < 4; ++j) red[j][tid] += red[j][tid + h];
+        __syncthreads();
+    }
+    if (tid < 4 && live) {
+        const double v = sqrt(red[tid][0]);
+        pnorm[(size_t)tid * n + o] = v;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        if (b > *reinterpret_cast<volatile unsigned long long*>(&colmax[tid])) atomicMax(&colmax[tid], b);
+    }
+}
+
 __global__ void k_row_eps(const double* __restrict__ pnorm, const unsigned long long* __restrict__ colmax, int n,
                           int d, int keff, double* __restrict__ row_eps) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -915,6 +1008,21 @@ static Shape shape_of(int d) {
     return s;
 }
 
+// The split-FP8 shape: K loop over 128-byte K blocks of e4m3 (A = [hi | lo | hi], B = [hi | hi | lo]),
+// 32 elements per MMA step.
+static Shape shape_fp8(int d) {
+    Shape s{};
+    const int kp = (3 * d + 127) / 128 * 128;
+    s.resident = false;
+    s.compact = false;
+    s.kpa = s.kpb = kp;
+    s.nkb_a = s.nkb_b = kp / 128;
+    s.ksteps = (3 * d + 31) / 32;
+    s.k1s = s.ksteps;
+    s.keff = 3 * d;
+    return s;
+}
+
 static size_t fixed_smem(const Shape& sh, int cap) {
     const int bcap = cap <= 32 ? 64 : 128;
     return 1024 + (sh.resident ? (size_t)sh.nkb_a * A_KB_BYTES : 0) + (size_t)(BLOCK_M + 1) * bcap * 8 + sizeof(Barriers);
@@ -929,10 +1037,16 @@ bool supported(int d, int cap) {
     return fixed_smem(sh, cap) + stage_smem(sh) <= 227 * 1024;  // at least one stage
 }
 
-size_t workspace_bytes(int n, int d) {
+bool supported_fp8(int d, int cap) {
+    if (d < 1 || cap < 1 || cap > 64 || 3 * d <= 128) return false;
+    const Shape sh = shape_fp8(d);
+    return fixed_smem(sh, cap) + stage_smem(sh) <= 227 * 1024;
+}
+
+size_t workspace_bytes(int n, int d, bool fp8) {
     const size_t np = (size_t)(n + 255) / 256 * 256;
-    const Shape sh = shape_of(d);
-    return np * (size_t)(sh.kpa + sh.kpb) * 2 + 4 * (size_t)n * 8 + (size_t)n * 8 + 4 * 8 + 4096;
+    const Shape sh = fp8 ? shape_fp8(d) : shape_of(d);
+    return np * (size_t)(sh.kpa + sh.kpb) * (fp8 ? 1 : 2) + 4 * (size_t)n * 8 + (size_t)n * 8 + 4 * 8 + 4096;
 }
 
 namespace {
@@ -948,33 +1062,38 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-bool make_map(CUtensorMap* m, const void* base, int kp, int rows, int box_rows) {
+// A 2-D map of an operand ([rows][kp] elements of bf16 or e4m3 bytes) with 128-byte boxes of
+// box_rows rows (one K block: 64 bf16 or 128 e4m3).
+bool make_map(CUtensorMap* m, const void* base, int kp, int rows, int box_rows, bool fp8 = false) {
     auto fn = encode_fn();
     if (!fn) return false;
+    const int esize = fp8 ? 1 : 2;
     cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kp * esize};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+    return fn(m, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base),
+              dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 struct Layout {
-    __nv_bfloat16 *opa, *opb;
+    void *opa, *opb;
     double *pnorm, *row_eps;
     unsigned long long* colmax;
 };
 
-Layout carve(void* ws, int n, int d) {
+Layout carve(void* ws, int n, int d, bool fp8) {
     const size_t np = (size_t)(n + 255) / 256 * 256;
-    const Shape sh = shape_of(d);
+    const Shape sh = fp8 ? shape_fp8(d) : shape_of(d);
+    const size_t esize = fp8 ? 1 : 2;
     char* p = static_cast<char*>(ws);
     Layout L;
-    L.opa = reinterpret_cast<__nv_bfloat16*>(p);
-    p += np * (size_t)sh.kpa * 2;
-    L.opb = reinterpret_cast<__nv_bfloat16*>(p);
-    p += np * (size_t)sh.kpb * 2;
+    L.opa = p;
+    p += np * (size_t)sh.kpa * esize;
+    L.opb = p;
+    p += np * (size_t)sh.kpb * esize;
     L.pnorm = reinterpret_cast<double*>(p);
     p += 4 * (size_t)n * 8;
     L.row_eps = reinterpret_cast<double*>(p);
@@ -985,29 +1104,35 @@ Layout carve(void* ws, int n, int d) {
 }  // namespace
 
 cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, const uint32_t* perm, cudaStream_t st,
-                    Plan& plan) {
+                    Plan& plan, bool fp8) {
     (void)dp;
     const int np = (n + 255) / 256 * 256;  // the tensor tiles are 256 columns wide
-    const Shape sh = shape_of(d);
-    Layout L = carve(ws, n, d);
+    const Shape sh = fp8 ? shape_fp8(d) : shape_of(d);
+    Layout L = carve(ws, n, d, fp8);
     cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
     if (e != cudaSuccess) return e;
     // xsT has ⌈n/128⌉·128 columns; operand rows in [n, np) are zero-filled by k_split itself.
     const size_t smem = (size_t)SPLIT_ROWS * (sh.kpa / 2 + 1 + sh.kpb / 2 + 1) * 4;
-    if (smem <= 227 * 1024) {
+    if (fp8) {
+        k_split_wide_fp8<<<np, 256, 0, st>>>(xsT, n, np_x, d, sh.kpa, perm, static_cast<uint8_t*>(L.opa),
+                                              static_cast<uint8_t*>(L.opb), L.pnorm, L.colmax);
+    } else if (smem <= 227 * 1024) {
         e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, sh.kpa, sh.kpb,
-                                                            sh.compact ? sh.k1s * 16 : 0, perm, L.opa, L.opb,
-                                                            L.pnorm, L.colmax);
+                                                            sh.compact ? sh.k1s * 16 : 0, perm,
+                                                            static_cast<__nv_bfloat16*>(L.opa),
+                                                            static_cast<__nv_bfloat16*>(L.opb), L.pnorm, L.colmax);
     } else {  // (deep rows: never the compact shape)
-        k_split_wide<<<np, 256, 0, st>>>(xsT, n, np_x, d, sh.kpa, perm, L.opa, L.opb, L.pnorm, L.colmax);
+        k_split_wide<<<np, 256, 0, st>>>(xsT, n, np_x, d, sh.kpa, perm, static_cast<__nv_bfloat16*>(L.opa),
+                                         static_cast<__nv_bfloat16*>(L.opb), L.pnorm, L.colmax);
     }
     note_launch();
     k_row_eps<<<(n + 255) / 256, 256, 0, st>>>(L.pnorm, L.colmax, n, d, sh.keff, L.row_eps); note_launch();
     plan.n = n;
     plan.d = d;
     plan.np = np;
+    plan.fp8 = fp8;
     plan.kpa = sh.kpa;
     plan.kpb = sh.kpb;
     plan.ops_a = L.opa;
@@ -1024,9 +1149,10 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
                           cudaStream_t st, int qb0, int qb1) {
     (void)sm_count;
     CUtensorMap ma, mb;
-    if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M) || !make_map(&mb, plan.ops_b, plan.kpb, plan.np, BLOCK_N))
+    if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M, plan.fp8) ||
+        !make_map(&mb, plan.ops_b, plan.kpb, plan.np, BLOCK_N, plan.fp8))
         return cudaErrorInvalidValue;
-    const Shape sh = shape_of(plan.d);
+    const Shape sh = plan.fp8 ? shape_fp8(plan.d) : shape_of(plan.d);
     const size_t fixed = fixed_smem(sh, cap), per = stage_smem(sh);
     int stages = 4;
     while (stages > 1 && fixed + (size_t)stages * per > 227 * 1024) --stages;
@@ -1035,8 +1161,10 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
     if (qb1 < 0) qb1 = qblocks;
     if (qb0 < 0 || qb1 > qblocks || qb0 >= qb1) return cudaErrorInvalidValue;
-    auto kern = !sh.resident ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
-                             : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
+    auto kern = plan.fp8 ? (cap <= 32 ? k_coarse_tc<1, true, true> : k_coarse_tc<2, true, true>)
+                : !sh.resident ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
+                               : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
+    if (plan.fp8 && sh.resident) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,

@@ -13,7 +13,8 @@ constexpr int BLOCK_N = 256;  // columns per tile (the MMA's N)
 
 struct Plan {
     int n, d, np;           // rows, features, padded rows
-    int kpa, kpb;           // row lengths (bf16) of the split operands
+    bool fp8;               // e4m3 operands (the split-FP8 kind) instead of bf16
+    int kpa, kpb;           // row lengths (elements: bf16, or e4m3 bytes) of the split operands
     const void* ops_a;      // [np][kpa] bf16 query operand  (hi | hi | lo, or hi | lo | hi for deep rows)
     const void* ops_b;      // [np][kpb] bf16 column operand (hi | lo, or hi | hi | lo for deep rows)
     const double* row_eps;  // [n] certificate bound of each query row
@@ -22,11 +23,14 @@ struct Plan {
 };
 
 bool supported(int d, int cap);
-size_t workspace_bytes(int n, int d);
+// The split-FP8 kind (e4m3 pieces of the rows scaled by 2^8, three products per pair, K loop): for
+// rows deep enough that the query tile is streamed (3d > 128), cap ≤ 64.
+bool supported_fp8(int d, int cap);
+size_t workspace_bytes(int n, int d, bool fp8 = false);
 // Split the normalised rows (xsT, d_pad × n_pad) into BF16 operands and per-row error norms, and
 // derive each row's certificate bound.
 cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, const uint32_t* perm, cudaStream_t st,
-                    Plan& plan);
+                    Plan& plan, bool fp8 = false);
 // All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
 // With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]);
 // with list_ub (their bounds, non-increasing) it stops once no later block can hold an admissible

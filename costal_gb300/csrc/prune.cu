@@ -345,6 +345,8 @@ __device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk
                     const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
                     v[j] = keep_max ? hi : lo;
                 }
+            } else if (stride == 16) {
+                if constexpr (KPT > 16) cx_regs<16>(v, base, size);
             } else if (stride == 8) {
                 if constexpr (KPT > 8) cx_regs<8>(v, base, size);
             } else if (stride == 4) {

@@ -32,8 +32,12 @@ extern "C" {
 
 /* Coarse-pass backends. Like the reference's `matmul` knob (crates/costal-core/src/matmul.rs:10-50)
  * they change speed only, never the output. */
-#define COSTAL_BACKEND_FP32 0  /* plain FP32 CUDA-core tiles: the default drop-in */
-#define COSTAL_BACKEND_BF16 1  /* certified split-BF16 tcgen05 tiles, FP32 accumulate in TMEM */
+#define COSTAL_BACKEND_FP32 0    /* plain FP32 CUDA-core tiles: the default drop-in */
+#define COSTAL_BACKEND_BF16 1    /* certified tcgen05 tiles, FP32 accumulate in TMEM: split BF16, or split
+                                    FP8 e4m3 for d >= 512 */
+#define COSTAL_BACKEND_BF16X3 2  /* certified split-BF16 tcgen05 tiles at every depth */
+#define COSTAL_BACKEND_FP8 3     /* certified split-FP8 (e4m3) tcgen05 tiles wherever the query tile is
+                                    streamed (3d > 128); split BF16 below that */
 
 #define COSTAL_SELECT_COSINE 0
 #define COSTAL_SELECT_TANIMOTO 1
@@ -74,6 +78,7 @@ typedef struct costal_knn_stats {
     double max_err_ratio;      /* max over the rescored candidates of |coarse - f64 score| divided by the
                                   bound the row's certificate used (E_i on the bf16 backend, the FP32
                                   epsilon otherwise): the certificate is sound while this stays below 1 */
+    uint64_t coarse_kind;      /* the coarse pass that ran: 0 FP32 tiles, 1 split BF16, 2 split FP8 */
 } costal_knn_stats;
 
 /* ---- module surface (crates/costal-py/src/lib.rs:80-102, 430-446) ---------------------------- */

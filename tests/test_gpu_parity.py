@@ -484,7 +484,7 @@ def test_certificate_bound_holds_on_adversarial_rows(ext, oracle, kind, d):
     n = 2000 if d < 2000 else 1200
     x = adversarial_rows(kind, n, d, 100 + d)
     want = oracle.knn_bruteforce(x, 10)
-    for backend in ("bf16", "fp32"):
+    for backend in ("bf16", "fp32", "fp8"):
         (idx, cos, norms), st = ext._knn_exact(x, 10, margin=54, matmul=backend)
         same(as_oracle((idx, cos, norms)), want)
         print(f"{kind} d={d} {backend}: max |coarse - exact| {st['max_coarse_err']:.3g}, "
@@ -530,3 +530,41 @@ def test_tanimoto_norm_window(ext, oracle, n, d, k, spread, signed):
           f"{st['blocks_total']} tiles, regathered {st['fallback_rows']}")
     if not signed and spread >= 6.0:
         assert st["blocks_skipped"] > 0.2 * st["blocks_total"], st
+
+
+@pytest.mark.parametrize("d", [130, 512, 2000])
+def test_split_fp8_kind(ext, oracle, d):
+    """The split-FP8 kind (e4m3 pieces of the rows scaled by 2^8, kind::f8f6f4 MMAs, 64 candidates a
+    row): on deep scRNA-like rows the answer equals the oracle's and the plain FP32 path's bit for
+    bit, every rescored candidate's error stays inside its row's bound, and the default tensor-core
+    backend picks this kind from d = 512 on."""
+    from costal_gb300 import workloads as W
+
+    x = W.scrna_100k(n=6000, d=d)
+    want, _ = oracle.knn_exact(x, 15)
+    (idx, cos, norms), st = ext._knn_exact(x, 15, matmul="fp8")
+    same(as_oracle((idx, cos, norms)), want)
+    assert st["coarse_kind"] == "fp8" and st["max_err_ratio"] < 1.0, st
+    _, st_auto = ext._knn_exact(x, 15, matmul="bf16")
+    assert st_auto["coarse_kind"] == ("fp8" if d >= 512 else "bf16")
+    (i3, c3, _), st3 = ext._knn_exact(x, 15, matmul="bf16x3")
+    same(as_oracle((i3, c3, norms)), want)
+    assert st3["coarse_kind"] == "bf16"
+    print(f"d={d}: fp8 recomputed {st['recomputed_rows']} of {len(x)} rows, max err / bound "
+          f"{st['max_err_ratio']:.3g}, max err {st['max_coarse_err']:.3g}")
+
+
+@pytest.mark.timeout(1800)
+def test_early_stop_beyond_8192_column_blocks(ext):
+    """2,200,000 rows of the Zipf generator: 8,594 column blocks of 256, past the 8,192 keys one list
+    sort of 16 keys a thread holds; the lists are sorted with 32 keys a thread (up to 16,384 blocks),
+    so the exact early stop still leaves blocks out, and every row equals the plain FP32 path's."""
+    from costal_gb300 import workloads as W
+
+    x = W.zipf_2m(n=2_200_000)
+    (idx, cos, norms), st = ext._knn_exact(x, 10, matmul="bf16")
+    assert st["blocks_stopped"] > 0.5 * st["blocks_total"], st
+    (fidx, fcos, fnorms), _ = ext._knn_exact(x, 10, matmul="fp32")
+    np.testing.assert_array_equal(idx, fidx)
+    np.testing.assert_array_equal(cos, fcos)
+    print(f"n=2,200,000: stopped {st['blocks_stopped']} of {st['blocks_total']} tiles")
