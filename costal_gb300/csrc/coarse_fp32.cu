@@ -411,6 +411,14 @@ __global__ void __launch_bounds__(NT, 1)
         L_s[e] = -CUDART_INF_F;
         L_i[e] = 0xffffffffu;
     }
+    // this thread's 8 query rows: f32 norm a and 1/a (constant over the tiles)
+    float a8[8], ia8[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int r = row_of(i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+        a8[i] = r < n ? tnW[r].x : 0.0f;
+        ia8[i] = a8[i] > 0.0f ? 1.0f / a8[i] : 0.0f;
+    }
     bool win_ok = false;  // every row's window is defined (its list is full and τ > 0)
     double win_lo = 0.0, win_hi = 0.0;
     int scanned = 0;
@@ -446,7 +454,43 @@ __global__ void __launch_bounds__(NT, 1)
             const int r = row_of(i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
             rows8[i] = r < n ? r : -1;
         }
-        tani_tile(acc, tnW, c0, n, tx, ty, rows8);
+        // A cosine prefilter (knn.rs:239-252 `tile_threshold`): with c = τ/(1+τ) > 0, a column of norm b
+        // can reach T > τ only if its cosine exceeds c·(b/a + a/b), and over this tile b/a + a/b is at
+        // least m (2 when the tile's norm range holds a, else its nearer end). Below c·m·(1 − 2⁻¹⁶) no
+        // entry of the row can be admitted (the margin covers every f32 rounding of T and of the
+        // threshold), so the divisions of T are spent only on a thread whose tile rows have a hit.
+        {
+            const float blo = (float)tile_lo[tile], bhi = (float)tile_hi[tile];
+            const float iblo = 1.0f / blo, ibhi = 1.0f / bhi;  // (+inf for a zero norm: unused then)
+            bool hit = false;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const float tau = tau_s[i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4)];
+                float thr = -CUDART_INF_F;
+                if (tau > 0.0f && rows8[i] >= 0) {
+                    if (a8[i] > 0.0f) {
+                        // (few-ulp roundings and the fast quotient all sit inside the 2⁻¹⁶ margin)
+                        const float rlo = blo * ia8[i], rhi = bhi * ia8[i];
+                        const float m = (rlo <= 1.0f && rhi >= 1.0f) ? 2.0f
+                                        : (rhi < 1.0f ? rhi + a8[i] * ibhi : rlo + a8[i] * iblo);
+                        thr = __fdividef(tau, 1.0f + tau) * m * (1.0f - 0x1p-16f);
+                    } else {
+                        thr = CUDART_INF_F;  // a zero row: T = 0 ≤ τ with every column
+                    }
+                }
+                const float m01 = fmaxf(acc[i][0], acc[i][1]), m23 = fmaxf(acc[i][2], acc[i][3]);
+                const float m45 = fmaxf(acc[i][4], acc[i][5]), m67 = fmaxf(acc[i][6], acc[i][7]);
+                hit |= fmaxf(fmaxf(m01, m23), fmaxf(m45, m67)) > thr;
+            }
+            if (hit) {
+                tani_tile(acc, tnW, c0, n, tx, ty, rows8);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = -CUDART_INF_F;
+            }
+        }
         select_tile<SLOTS>(acc, c0, n, cap, L_s, L_i, buf_s, buf_i, cnt_s, len_s, tau_s, floor_s, warp, lane, tx, ty,
                            row_of, [&](int qi, int cl) {
                                float sv = 0.0f;
