@@ -177,6 +177,89 @@ def cpu_baseline(x, wl, target_s=15.0, threads=0):
     return rows / dt, cores, f"{rows} query rows x all {n} columns (kNN incl. f64 rescoring), {dt:.1f} s"
 
 
+def cpu_crosscheck(x, wl, sampled, args):
+    """The CPU port on one thread (a sample of rows), and in full on 200,000- and 400,000-row draws of
+    the same generator, extrapolated by n^2 to the workload's n: a check of the sampled all-core
+    figure."""
+    from costal_gb300 import workloads as W
+    from oracle import oracle as O
+
+    v1, _, s1 = cpu_baseline(x, wl, target_s=args.cpu_seconds, threads=1)
+    full = {}
+    for m in (200_000, 400_000):
+        xm = W.make(wl.name, n=m)[0]
+        t = time.perf_counter()
+        O.knn_exact(xm, wl.k, margin=wl.margin)
+        full[m] = time.perf_counter() - t
+    est = {m: full[m] * (wl.n / m) ** 2 for m in full}
+    return {"one_core_value": v1, "one_core_sample": s1,
+            "full_runs_s": {str(m): full[m] for m in full},
+            "extrapolated_s_at_n": {str(m): est[m] for m in est},
+            "extrapolated_cells_per_s": {str(m): wl.n / est[m] for m in est},
+            "sampled_cells_per_s": sampled}
+
+
+def _hubs(spokes, d=64, seed=8):
+    """Two centres, each the nearest neighbour of half the spokes (long rows in the Leiden CSR)."""
+    rng = np.random.default_rng(seed)
+    u = rng.normal(size=(spokes, d))
+    side = np.arange(spokes) % 2
+    u[np.arange(spokes), side] = 0.0
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    return np.ascontiguousarray(np.vstack([np.eye(d)[:2], np.eye(d)[side] + 0.3 * u]), dtype=np.float32)
+
+
+def _profile_case(name):
+    from costal_gb300 import _costal as ext
+    from costal_gb300 import workloads as W
+
+    if name in ("coarse_fp32_kc", "split_wide", "coarse_tc_fp8"):
+        x = W.scrna_100k(n=20_000)
+        matmul = {"coarse_fp32_kc": "fp32", "split_wide": "bf16x3", "coarse_tc_fp8": "fp8"}[name]
+        return [lambda: ext._knn_exact(x, 15, matmul=matmul)[1]]
+    if name == "gather":  # integer rows: ties everywhere, every row regathered
+        x = np.floor(np.random.default_rng(5).uniform(0, 3, size=(50_000, 6))).astype(np.float32)
+        return [lambda: ext._knn_exact(x, 12)[1]]
+    if name == "merge_parts":  # 300 near-identical rows fail the split-BF16 certificate
+        x = W.mixture_20k(n=200_000, d=16)
+        rng = np.random.default_rng(9)
+        base = rng.uniform(0, 1, size=(1, 16))
+        x[:300] = (base * (1 + 1e-6 * rng.standard_normal((300, 16)))).astype(np.float32)
+        return [lambda: ext._knn_exact(np.ascontiguousarray(x), 10, matmul="bf16")[1]]
+    if name == "tanimoto_window":
+        x, wl = W.make("rare_400k", n=200_000)
+        return [lambda: ext._knn_exact(x, wl.k, margin=wl.margin, select="tanimoto")[1]]
+    if name == "jaccard":
+        x = W.mixture_20k(n=400_000)
+        idx, cos, norms = ext._knn_exact(x, 10)[0]
+        return [lambda: {"shape": ext._reweight(idx, cos, norms, "jaccard").shape}]
+    if name == "csr":
+        x = _hubs(12_000)
+        return [lambda: {"nnz": len(ext._build_graph_csr(x, 15)[1])}]
+    raise ValueError(name)
+
+
+PROFILE_CASES = {
+    "coarse_fp32_kc": "k_coarse_fp32_kc: the FP32 pass for deep rows (20,000 x 2,000 scRNA-like)",
+    "split_wide": "k_split_wide: the split-BF16 operands of deep rows (20,000 x 2,000)",
+    "coarse_tc_fp8": "k_coarse_tc<.., FP8>: the split-FP8 tensor-core pass (20,000 x 2,000)",
+    "gather": "k_gather: the full-row regather (50,000 x 6 integer rows)",
+    "merge_parts": "k_merge_parts: column-segment lists of re-run rows merged (200,000 x 16, 300 near-copies)",
+    "tanimoto_window": "k_coarse_tani_window: Tanimoto selection with the norm window (200,000 x 15)",
+    "jaccard": "k_sort_rows + k_jaccard: Jaccard weights (400,000 x 10 neighbours)",
+    "csr": "k_sort_big + k_csr_emit: the Leiden CSR with two hub rows of ~6,000 entries",
+}
+
+
+def run_profile_case(name):
+    calls = _profile_case(name)
+    for _ in range(2):
+        out = calls[0]()
+    keep = ("coarse_kind", "recomputed_rows", "fallback_rows", "blocks_skipped", "blocks_total", "ms_kernel")
+    print(json.dumps({"profile_case": name, "what": PROFILE_CASES[name],
+                      "result": {k_: v for k_, v in out.items() if k_ in keep or k_ in ("shape", "nnz")}}))
+
+
 def run_reference(args, wl, x):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -221,8 +304,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-crosscheck", action="store_true",
+                    help="also time the CPU port on one thread and in full at n = 200,000 and 400,000 (n^2 check)")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
+                    help="run one small case that launches the named kernel twice (for ncu captures) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
 
     from costal_gb300 import workloads as W
 
@@ -496,6 +585,8 @@ def main():
         if not args.no_cpu:
             v, cores, sample = cpu_baseline(x, wl, target_s=args.cpu_seconds)
             line["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample}
+            if args.cpu_crosscheck:
+                line["cpu_baseline"]["crosscheck"] = cpu_crosscheck(x, wl, v, args)
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

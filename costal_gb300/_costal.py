@@ -342,6 +342,23 @@ def _leiden_many(n, rows, cols, weights, *, resolutions, seeds, beta=0.01, n_ite
     return out.view(np.int32)
 
 
+def _leiden_many_csr(n, indptr, nbr, weights, *, resolutions, seeds, beta=0.01, n_iterations=2, n_threads=None):
+    """GB300 addition: _leiden_many on the CSR _build_graph_csr returns, used in place (the same labels
+    as _leiden_many on the edge list the CSR was built from) -> int32 (runs, n)."""
+    n = _u64(n, "n")
+    indptr = _arr(indptr, np.uint64, 1, "indptr")
+    nbr = _arr(nbr, np.uint32, 1, "nbr")
+    w = _arr(weights, np.float64, 1, "weights")
+    if len(indptr) != n + 1:
+        raise ValueError(f"indptr has {len(indptr)} entries for n={n}")
+    res = np.ascontiguousarray([float(v) for v in resolutions], dtype=np.float64)
+    sd = np.ascontiguousarray([_u64(v, "seed") for v in seeds], dtype=np.uint64)
+    out = np.empty((len(res) * len(sd), n), np.uint32)
+    _call(L.lib().costal_leiden_many_csr, n, _ptr(indptr), _ptr(nbr), _ptr(w), _ptr(res), len(res), _ptr(sd), len(sd),
+          float(beta), int(n_iterations), int(n_threads or 0), _ptr(out))
+    return out.view(np.int32)
+
+
 def _leiden_coo(n, rows, cols, weights, *, objective, resolution, beta, n_iterations, seed, initial=None,
                 n_threads=None):
     """lib.rs:352-412: Leiden on an external COO list -> (labels int64, quality, n_clusters, iterations, converged)."""

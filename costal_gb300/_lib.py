@@ -115,6 +115,7 @@ SIGNATURES = {
     "costal_leiden": [U64, P, P, P, U64, INT, INT, DBL, DBL, I32, U64, P, P, P, P, P, P, STR, SZ],
     "costal_leiden_csr": [U64, P, P, P, INT, DBL, DBL, I32, U64, P, P, P, P, P, P, STR, SZ],
     "costal_leiden_many": [U64, P, P, P, U64, P, U64, P, U64, DBL, I32, INT, P, STR, SZ],
+    "costal_leiden_many_csr": [U64, P, P, P, P, U64, P, U64, DBL, I32, INT, P, STR, SZ],
     "costal_modularity": [U64, P, P, P, U64, P, DBL, P, STR, SZ],
     "costal_reweight_jaccard_device_noalloc": [P, U64, U32, P, P, STR, SZ],
     "costal_knn_shard_device": [P, U64, U32, U32, P, U32, U32, P, P, P, P, P, P, P, P, STR, SZ],

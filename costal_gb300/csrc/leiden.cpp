@@ -830,15 +830,13 @@ int costal_leiden_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, c
     return COSTAL_OK;
 }
 
-int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
-                       const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
-                       double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen) {
+namespace {
+// lib.rs:311-350: every (resolution, seed) run on one graph, resolutions outer; runs in parallel,
+// each deterministic.
+int many_runs(const Csr& g, uint64_t n, const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds,
+              uint64_t n_seeds, double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err,
+              size_t errlen) {
     std::string e;
-    Csr g;
-    if (!csr_from_edges(n, rows, cols, weights, m, g, e)) {
-        put_err(err, errlen, e);
-        return COSTAL_EINVAL;
-    }
     size_t runs = (size_t)n_resolutions * n_seeds;
     for (size_t r = 0; r < n_resolutions; ++r)
         if (!check_params(0, resolutions[r], beta, n_iterations, e)) {
@@ -863,6 +861,31 @@ int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, c
         }
     }
     return COSTAL_OK;
+}
+}  // namespace
+
+int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
+                       const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
+                       double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen) {
+    std::string e;
+    Csr g;
+    if (!csr_from_edges(n, rows, cols, weights, m, g, e)) {
+        put_err(err, errlen, e);
+        return COSTAL_EINVAL;
+    }
+    return many_runs(g, n, resolutions, n_resolutions, seeds, n_seeds, beta, n_iterations, n_threads, out, err, errlen);
+}
+
+int costal_leiden_many_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, const double* weights,
+                           const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
+                           double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen) {
+    std::string e;
+    Csr g;
+    if (!csr_view(n, indptr, nbr, weights, g, e)) {
+        put_err(err, errlen, e);
+        return COSTAL_EINVAL;
+    }
+    return many_runs(g, n, resolutions, n_resolutions, seeds, n_seeds, beta, n_iterations, n_threads, out, err, errlen);
 }
 
 int costal_modularity(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,

@@ -225,6 +225,11 @@ int costal_leiden_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, c
 int costal_leiden_many(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
                        const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
                        double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen);
+/* GB300 addition: lib.rs:311-350 `_leiden_many` on a graph given in the CSR layout of costal_leiden_csr
+   (as costal_build_graph_csr produces it), used in place: the same labels as on its edge list. */
+int costal_leiden_many_csr(uint64_t n, const uint64_t* indptr, const uint32_t* nbr, const double* weights,
+                           const double* resolutions, uint64_t n_resolutions, const uint64_t* seeds, uint64_t n_seeds,
+                           double beta, int32_t n_iterations, int n_threads, uint32_t* out, char* err, size_t errlen);
 /* lib.rs:416-428 `_modularity`. */
 int costal_modularity(uint64_t n, const uint32_t* rows, const uint32_t* cols, const double* weights, uint64_t m,
                       const uint32_t* membership, double resolution, double* q, char* err, size_t errlen);

@@ -568,3 +568,21 @@ def test_early_stop_beyond_8192_column_blocks(ext):
     np.testing.assert_array_equal(idx, fidx)
     np.testing.assert_array_equal(cos, fcos)
     print(f"n=2,200,000: stopped {st['blocks_stopped']} of {st['blocks_total']} tiles")
+
+
+def test_leiden_ensemble_on_the_device_graph(ext, oracle):
+    """_leiden_many (lib.rs:311-350, the ensemble of find_communities_multiscale, _multiscale.py:170-175)
+    fed the GPU-built graph, as an edge list and as the device-built CSR used in place: the labels of
+    every (resolution, seed) run equal the ensemble's on the oracle's graph of the same input."""
+    from costal_gb300 import workloads as W
+
+    x, wl = W.make("mixture_20k")
+    res, seeds = [0.2, 0.8, 1.6, 3.2], [0, 1, 2]
+    (oidx, ocos, onorms), _ = oracle.knn_exact(x, wl.k)
+    orows, ocols, ow = oracle.fuzzy_union(oidx, oracle.reweight(oidx, ocos, onorms, "tanimoto"))
+    want = ext._leiden_many(len(x), orows.view(np.int32), ocols.view(np.int32), ow, resolutions=res, seeds=seeds)
+    for matmul in ("fp32", "bf16"):
+        rows, cols, w = ext._build_graph(x, wl.k, matmul=matmul)
+        np.testing.assert_array_equal(ext._leiden_many(len(x), rows, cols, w, resolutions=res, seeds=seeds), want)
+        indptr, nbr, cw = ext._build_graph_csr(x, wl.k, matmul=matmul)
+        np.testing.assert_array_equal(ext._leiden_many_csr(len(x), indptr, nbr, cw, resolutions=res, seeds=seeds), want)

@@ -125,3 +125,13 @@ def test_csr_entry_matches_the_edge_list_and_checks_its_input(ext):
         ext._leiden_csr(n, indptr, nbr, ww, resolution=1.0)
     with pytest.raises(ValueError, match="entries"):
         ext._leiden_csr(n + 1, indptr, nbr, cw, resolution=1.0)
+
+
+def test_many_on_a_csr_matches_the_edge_list(ext):
+    """The ensemble of lib.rs:311-350 on a graph given as the Leiden's CSR (leiden.rs:52-101 of the
+    edge list, as the GPU builds it), used in place: the same labels as on the edge list."""
+    n, rows, cols, w = planted(seed=4)
+    many = ext._leiden_many(n, rows, cols, w, resolutions=[0.5, 1.0, 2.0], seeds=[0, 7])
+    indptr, nbr, cw = csr_from_edges(n, rows, cols, w)
+    got = ext._leiden_many_csr(n, indptr, nbr, cw, resolutions=[0.5, 1.0, 2.0], seeds=[0, 7])
+    np.testing.assert_array_equal(got, many)
