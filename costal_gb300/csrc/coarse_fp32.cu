@@ -499,8 +499,13 @@ __global__ void __launch_bounds__(NT, 1)
                                return tani_coarse_f32(sv, q < n ? tnW[q] : make_float2(0.0f, 0.0f),
                                                       col < n ? tnW[col] : make_float2(0.0f, 0.0f));
                            });
+        // The union of the rows' windows in absolute norms (knn.rs:668-678), in f64 (the GB300's slow
+        // pipe): until every row has one, after each tile; then after every eighth tile scanned. In
+        // between the tests use the last union, computed from lower thresholds, which only makes it
+        // wider (the windows shrink as τ rises): the stops may come a few tiles later, never too early.
+        const bool sides_open = (!rstop && right < all_tiles) || (!lstop && left >= 0);
+        if (!sides_open || (win_ok && (scanned & 7) != 1)) continue;
         __syncthreads();  // every query's τ after this tile
-        // The union of the rows' windows in absolute norms (knn.rs:668-678), in f64.
         if (tid < BM) {
             const int w = q0 + tid;
             double lo = CUDART_INF, hi = -CUDART_INF;
