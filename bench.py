@@ -306,6 +306,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--cpu-crosscheck", action="store_true",
                     help="also time the CPU port on one thread and in full at n = 200,000 and 400,000 (n^2 check)")
+    ap.add_argument("--sharded", action="store_true",
+                    help="time the multi-GPU (row-shard) step even on one GPU (a one-rank process group)")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
                     help="run one small case that launches the named kernel twice (for ncu captures) and exit")
     args = ap.parse_args()
@@ -327,10 +329,14 @@ def main():
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as dist
+    import torch.distributed as dist
 
+    if ws > 1:
         dist.init_process_group("nccl")
+    elif args.sharded:  # the sharded step on one rank (a one-process NCCL group)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29531")
+        dist.init_process_group("nccl", rank=0, world_size=1)
     from costal_gb300 import _lib as L
 
     lib = L.lib()
@@ -374,7 +380,7 @@ def main():
     m = C.c_uint64()
     st = L.KnnStats()
 
-    sharded = ws > 1
+    sharded = ws > 1 or args.sharded
     shard_stats = {}
 
     def step_sharded(o, xd):
@@ -588,7 +594,7 @@ def main():
             if args.cpu_crosscheck:
                 line["cpu_baseline"]["crosscheck"] = cpu_crosscheck(x, wl, v, args)
         print(json.dumps(line), flush=True)
-    if ws > 1:
+    if dist.is_initialized():
         dist.destroy_process_group()
 
 

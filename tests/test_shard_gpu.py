@@ -61,3 +61,32 @@ def test_device_union_rejects_bad_indices(ext):
     w = torch.ones((3, 2), dtype=torch.float64, device="cuda")
     with pytest.raises(ValueError, match="neighbor index 7 out of range"):
         S.union_device(idx, w)
+
+
+@pytest.mark.parametrize("backend", ["fp32", "bf16"])
+def test_sharded_build_through_nccl_on_one_rank(ext, backend):
+    """The multi-GPU step as bench.py and a user run it (shard, NCCL all-gather, device union) in a
+    one-rank process group: the same edges and kNN as the one-call graph."""
+    import socket
+
+    import torch
+    import torch.distributed as dist
+
+    from costal_gb300 import shard as S
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    dist.init_process_group("nccl", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        x = clustered(20_000, 24, 5)
+        (r, c, w), (idx, cos, norms), _ = S.build_graph_sharded(torch.from_numpy(x).cuda(), 10, matmul=backend)
+        er, ec, ew = ext._build_graph(x, 10, matmul=backend)
+        np.testing.assert_array_equal(r.cpu().numpy(), er)
+        np.testing.assert_array_equal(c.cpu().numpy(), ec)
+        np.testing.assert_array_equal(w.cpu().numpy(), ew)
+        (widx, wcos, wnorms), _ = ext._knn_exact(x, 10, matmul=backend)
+        np.testing.assert_array_equal(idx.cpu().numpy(), widx)
+        np.testing.assert_array_equal(cos.cpu().numpy(), wcos)
+    finally:
+        dist.destroy_process_group()
