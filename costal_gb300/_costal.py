@@ -452,6 +452,27 @@ def _mlp_forward(params, feat):
     return out
 
 
+def _block_bounds(x):
+    """Test hook: the tensor-core path's per-row block bound data for X (n, d), d <= 64.
+
+    Returns (perm, ccenter, cradius, rowmax, delta): the working order (working -> original row),
+    the unit centres (ncb, d) and angular radii (ncb,) of the column blocks of 256 working rows, the
+    largest split-BF16 coarse score of each query block's rows (blocks of 128) with each centre
+    (nqb, ncb), and that score's error margin in cosine.
+    """
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n, d = x.shape
+    nqb, ncb = (n + 127) // 128, (n + 255) // 256
+    perm = np.empty(n, np.uint32)
+    ccenter = np.empty((ncb, d), np.float64)
+    cradius = np.empty(ncb, np.float64)
+    rowmax = np.empty((nqb, ncb), np.float32)
+    delta = C.c_float()
+    _call(L.lib().costal_block_bounds, _ptr(x), n, d, _ptr(perm), _ptr(ccenter), _ptr(cradius), _ptr(rowmax),
+          C.byref(delta))
+    return perm, ccenter, cradius, rowmax, float(delta.value)
+
+
 def _mlp_gradient(params, feat, y, quantile):
     """Test hook: the GPU gradient of the mean pinball loss for given weights, features and labels."""
     params = np.ascontiguousarray(params, dtype=np.float32)

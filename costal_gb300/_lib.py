@@ -126,6 +126,7 @@ SIGNATURES = {
     "costal_mlp_clear": [STR, SZ],
     "costal_mlp_forward": [P, U32, P, U64, P, STR, SZ],
     "costal_mlp_gradient": [P, U32, P, P, U64, C.c_float, P, STR, SZ],
+    "costal_block_bounds": [P, U64, U32, P, P, P, P, P, STR, SZ],
 }
 
 _lib = None

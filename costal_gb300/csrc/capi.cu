@@ -69,7 +69,7 @@ struct Context {
     DevBuf fu_scratch, rows, cols, wout, idx_in, cos_in, norms_in, w_in, jac, f32out, tc_ws, tc_rows, prune_ws;
     DevBuf mlp_params, mlp_params_bf, mlp_m1, mlp_m2, mlp_feat, mlp_y, mlp_pred, mlp_partial, mlp_grad, mlp_rows;
     DevBuf part_idx, part_score, part_tau, tfloor;
-    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm, shard_rows, tani_perm, tani_ws;
+    DevBuf csr_ws, csr_indptr, csr_src, csr_nbr, csr_w, tnorm, shard_rows, tani_perm, tani_ws, rm_ws, rm_out;
     MlpState mlp;
 };
 
@@ -331,6 +331,23 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             if (ordered) {
                 CK(ensure(c.prune_ws, prune::workspace_bytes(n, d)));
                 CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), n, np, d, s, pp));
+            }
+            CK(ensure(c.tc_ws, tc::workspace_bytes(n, d, fp8)));
+            CK(ensure(c.tc_rows, (size_t)n * 4));
+            tc::Plan plan{};
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan, fp8));
+            if (ordered) {
+                // with the early stop, the lists take the per-row bound too (the nearest row of each
+                // query block to each column block's centre, from the split operands just made)
+                if (o.prune && tc::rowmax_supported(plan)) {
+                    CK(ensure(c.rm_ws, tc::rowmax_bytes(pp.ncb, d)));
+                    CK(ensure(c.rm_out, (size_t)pp.nqb * pp.ncb * 4));
+                    const float* delta = nullptr;
+                    CK(tc::launch_rowmax(plan, pp.ccenter_f, pp.ncb, c.rm_ws.p, c.rm_out.as<float>(), &delta,
+                                         &dm->timeout_flag, s));
+                    pp.rowmax = c.rm_out.as<float>();
+                    pp.rm_delta = delta;
+                }
                 learned = o.learned_prune && c.mlp.ready && c.mlp.d == d && c.mlp.k == k;
                 if (learned) {
                     CK(mlp_predict_thresholds(c, pp, s));
@@ -347,10 +364,6 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                     CK(launch_iota(srows, qb0 * 128, nrows, s));
             }
             CK(cudaEventRecord(c.ev[5], s));
-            CK(ensure(c.tc_ws, tc::workspace_bytes(n, d, fp8)));
-            CK(ensure(c.tc_rows, (size_t)n * 4));
-            tc::Plan plan{};
-            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan, fp8));
             CK(cudaEventRecord(c.ev[6], s));
             if (nrows > 0)
                 CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr,
@@ -1044,6 +1057,47 @@ int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, cons
                          c.mlp_partial.as<float>(), c.mlp_grad.as<float>(), s));
         CK(cudaMemcpyAsync(grad, c.mlp_grad.p, P * 4, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+    });
+}
+
+int costal_block_bounds(const float* x, uint64_t n, uint32_t d, uint32_t* perm, double* ccenter, double* cradius,
+                        float* rowmax, float* delta, char* err, size_t errlen) {
+    return guarded(err, errlen, [&](Context& c) {
+        if (n < 2 || n > (uint64_t)INT32_MAX / 2) throw Fail{COSTAL_EINVAL, "n out of range"};
+        if (!prune::supported((int)d)) throw Fail{COSTAL_EUNSUPPORTED, "block bounds cover 1 <= d <= 64"};
+        cudaStream_t s = c.stream;
+        const int N = (int)n, D = (int)d;
+        const int dp = coarse_dpad(D), np = round_up(N, 128);
+        CK(ensure(c.x, n * d * 4ull));
+        CK(ensure(c.norms, n * 8ull));
+        CK(ensure(c.xsT, (size_t)dp * np * 4));
+        CK(ensure(c.misc, sizeof(Misc)));
+        Misc* dm = c.misc.as<Misc>();
+        CK(cudaMemsetAsync(dm, 0, sizeof(Misc), s));
+        CK(cudaMemsetAsync(&dm->bad_row, 0xff, 8, s));
+        CK(cudaMemcpyAsync(c.x.p, x, n * d * 4ull, cudaMemcpyHostToDevice, s));
+        CK(launch_prep(c.x.as<float>(), N, D, np, dp, c.norms.as<double>(), c.xsT.as<float>(), &dm->bad_row, s));
+        CK(ensure(c.prune_ws, prune::workspace_bytes(N, D)));
+        prune::Plan pp{};
+        CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), N, np, D, s, pp));
+        CK(ensure(c.tc_ws, tc::workspace_bytes(N, D, false)));
+        tc::Plan plan{};
+        CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), N, np, dp, D, pp.perm, s, plan, false));
+        CK(ensure(c.rm_ws, tc::rowmax_bytes(pp.ncb, D)));
+        CK(ensure(c.rm_out, (size_t)pp.nqb * pp.ncb * 4));
+        const float* d_delta = nullptr;
+        CK(tc::launch_rowmax(plan, pp.ccenter_f, pp.ncb, c.rm_ws.p, c.rm_out.as<float>(), &d_delta, &dm->timeout_flag,
+                             s));
+        CK(cudaMemcpyAsync(perm, pp.perm, n * 4ull, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(ccenter, pp.ccenter, (size_t)pp.ncb * D * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(cradius, pp.cradius, (size_t)pp.ncb * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rowmax, c.rm_out.p, (size_t)pp.nqb * pp.ncb * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(delta, d_delta, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(c.h_misc, dm, sizeof(Misc), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (c.h_misc->bad_row != ~0ull)
+            throw Fail{COSTAL_EINVAL, "row " + std::to_string(c.h_misc->bad_row) + " contains NaN or inf"};
+        if (c.h_misc->timeout_flag) throw Fail{COSTAL_ETIMEOUT, "a bounded device wait in the bound kernel gave up"};
     });
 }
 

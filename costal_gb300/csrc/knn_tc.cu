@@ -737,6 +737,161 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
 }
 
+// ---- per-row block bounds --------------------------------------------------------------------------
+//
+// Every row x of column block B lies within angle r_B of B's unit centre c_B, so for a query row q,
+// cos(q, x) ≤ cos(max(0, angle(q, c_B) − r_B)). Over a query block Q the bound is loosest for the
+// row nearest c_B, so the block needs only M[Q][B] = max over q ∈ Q of q·c_B: a (centres × query
+// rows) product, run here with the coarse pass's split-BF16 operands. The centres take the A layout
+// (M = 128 centres per tile, one TMEM lane each) and the query block's rows the B layout (N = 128),
+// so every epilogue thread reduces its own centre's 128 accumulators in registers. One CTA per query
+// block: warp 4 loads the block's rows once and streams centre tiles into a ring of stages, warp 5
+// issues the MMAs into two 128-column accumulators, warps 0-3 reduce and write M[Q][·].
+constexpr int RM_N = 128;                       // query rows per tile (the MMA's N)
+constexpr int RM_KB_BYTES = 128 * 128;          // one 128-byte K block of 128 operand rows
+constexpr uint32_t RM_TMEM_COLS = 2 * RM_N;     // two accumulators
+constexpr uint32_t IDESC_RM = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(RM_N >> 3) << 17) |
+                              ((uint32_t)(BLOCK_M >> 4) << 24);
+
+struct __align__(8) RmBars {
+    uint64_t q_full;
+    uint64_t c_full[4];
+    uint64_t c_empty[4];
+    uint64_t t_full[2];
+    uint64_t t_empty[2];
+    uint32_t tmem_base;
+};
+
+__device__ __forceinline__ void mma_rm(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(IDESC_RM), "r"(accumulate)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_block_rowmax(const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_q, int n, int ncb,
+                   int nkb_c, int nkb_q, int ksteps, int k1s, int stages, float* __restrict__ rowmax,
+                   unsigned long long* __restrict__ timeout_flag) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t base_u32 = smem_u32(smem_raw);
+    unsigned char* smem = smem_raw + ((1024 - (base_u32 & 1023)) & 1023);  // 1024-byte aligned tiles
+    const uint32_t q_bytes = (uint32_t)nkb_q * RM_KB_BYTES, c_bytes = (uint32_t)nkb_c * RM_KB_BYTES;
+    unsigned char* q_tile = smem;                 // the query block's rows, resident
+    unsigned char* c_tiles = smem + q_bytes;      // stages × one centre tile
+    RmBars* bars = reinterpret_cast<RmBars*>(c_tiles + (size_t)stages * c_bytes);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int Q = (int)blockIdx.x, q0 = Q * RM_N;
+    const int ntiles = (ncb + BLOCK_M - 1) / BLOCK_M;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars->q_full, 1);
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&bars->c_full[s], 1);
+            mbar_init(&bars->c_empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&bars->t_full[b], 1);
+            mbar_init(&bars->t_empty[b], EPI_WARPS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == EPI_WARPS + 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&bars->tmem_base)),
+                     "r"(RM_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = bars->tmem_base;
+
+    if (warp == EPI_WARPS) {
+        if (lane == 0) {
+            mbar_expect_tx(&bars->q_full, q_bytes);
+            for (int kb = 0; kb < nkb_q; ++kb)
+                tma_load_2d(q_tile + (size_t)kb * RM_KB_BYTES, &map_q, kb * KB, q0, &bars->q_full);
+            for (int t = 0; t < ntiles; ++t) {
+                const int s = t % stages;
+                const uint32_t ph = (uint32_t)(t / stages) & 1u;
+                if (!mbar_wait(&bars->c_empty[s], ph ^ 1u, timeout_flag, true)) break;
+                mbar_expect_tx(&bars->c_full[s], c_bytes);
+                unsigned char* dst = c_tiles + (size_t)s * c_bytes;
+                for (int kb = 0; kb < nkb_c; ++kb)
+                    tma_load_2d(dst + (size_t)kb * RM_KB_BYTES, &map_c, kb * KB, t * BLOCK_M, &bars->c_full[s]);
+            }
+        }
+    } else if (warp == EPI_WARPS + 1) {
+        if (lane == 0) {
+            const bool ok = mbar_wait(&bars->q_full, 0, timeout_flag, true);
+            tc_fence_after();
+            const uint32_t q_base = smem_u32(q_tile);
+            for (int t = 0; ok && t < ntiles; ++t) {
+                const int s = t % stages, buf = t & 1;
+                const uint32_t ph = (uint32_t)(t / stages) & 1u, bph = (uint32_t)(t >> 1) & 1u;
+                if (!mbar_wait(&bars->t_empty[buf], bph ^ 1u, timeout_flag, true)) break;
+                if (!mbar_wait(&bars->c_full[s], ph, timeout_flag, true)) break;
+                tc_fence_after();
+                const uint32_t c_base = smem_u32(c_tiles + (size_t)s * c_bytes);
+                const uint32_t dt = tmem + (uint32_t)(buf * RM_N);
+                // the coarse pass's chains with the operands' roles swapped: the products are the
+                // same three pieces (hi·hi, hi·lo, lo·hi) of every (centre, row) pair
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const int kb = ks < k1s ? ks : ks - k1s;
+                    const uint64_t ad = sw128_desc(c_base + (uint32_t)(ks >> 2) * RM_KB_BYTES + (uint32_t)((ks & 3) * 32));
+                    const uint64_t bd = sw128_desc(q_base + (uint32_t)(kb >> 2) * RM_KB_BYTES + (uint32_t)((kb & 3) * 32));
+                    mma_rm(dt, ad, bd, ks > 0 ? 1u : 0u);
+                }
+                mma_commit(&bars->c_empty[s]);
+                mma_commit(&bars->t_full[buf]);
+            }
+        }
+    } else {
+        const int nv = min(RM_N, n - q0);  // live query rows of the block (the rest are zero rows)
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        uint32_t ra[64], rb[64];
+        for (int t = 0; t < ntiles; ++t) {
+            const int buf = t & 1;
+            const uint32_t bph = (uint32_t)(t >> 1) & 1u;
+            if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag, false)) break;
+            tc_fence_after();
+            const uint32_t tb = lane_addr + (uint32_t)(buf * RM_N);
+            tmem_ld64(tb, ra);
+            tmem_ld64(tb + 64, rb);
+            tmem_wait(ra);
+            tmem_wait(rb);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bars->t_empty[buf]);
+            if (nv < RM_N) {  // the last block: rows past n do not count
+#pragma unroll
+                for (int j = 0; j < 64; ++j) {
+                    if (j >= nv) ra[j] = __float_as_uint(-CUDART_INF_F);
+                    if (64 + j >= nv) rb[j] = __float_as_uint(-CUDART_INF_F);
+                }
+            }
+            float m0 = -CUDART_INF_F, m1 = -CUDART_INF_F, m2 = -CUDART_INF_F, m3 = -CUDART_INF_F;
+#pragma unroll
+            for (int j = 0; j < 64; j += 4) {
+                m0 = max3f(m0, __uint_as_float(ra[j]), __uint_as_float(rb[j]));
+                m1 = max3f(m1, __uint_as_float(ra[j + 1]), __uint_as_float(rb[j + 1]));
+                m2 = max3f(m2, __uint_as_float(ra[j + 2]), __uint_as_float(rb[j + 2]));
+                m3 = max3f(m3, __uint_as_float(ra[j + 3]), __uint_as_float(rb[j + 3]));
+            }
+            const int c = t * BLOCK_M + warp * 32 + lane;
+            if (c < ncb) rowmax[(size_t)Q * ncb + c] = fmaxf(fmaxf(m0, m1), fmaxf(m2, m3));
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == EPI_WARPS + 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(RM_TMEM_COLS) : "memory");
+    }
+}
+
 // ---- operand preparation ----------------------------------------------------------------------
 
 // One CTA per 128 working rows: each thread splits its row (read from xsT at the original index)
@@ -1170,6 +1325,102 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,
                                             cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, plan.row_eps,
                                             cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0); note_launch();
+    return cudaGetLastError();
+}
+
+// The margin of the row bounds' coarse scores, in cosine: k_row_eps's split-remainder and
+// accumulation terms with the maxima of both sides' piece norms (the centres and the rows; the bound
+// is symmetric in the two operands), plus (2d + 8)·2⁻²³ for the f32 rows' norms (within (d + 2)·2⁻²⁴
+// of 1) and the centres' rounding to f32 (2⁻²⁴), rounded up to f32.
+__global__ void k_rowmax_delta(const unsigned long long* __restrict__ cm_c, const unsigned long long* __restrict__ cm_r,
+                               int d, int keff, float* __restrict__ delta) {
+    if (threadIdx.x != 0) return;
+    const double up = 1.0 + 1e-12;
+    double c[4], r[4];
+    for (int j = 0; j < 4; ++j) {
+        c[j] = __longlong_as_double((long long)cm_c[j]) * up;
+        r[j] = __longlong_as_double((long long)cm_r[j]) * up;
+    }
+    // [0] ‖hi‖, [1] ‖lo‖, [2] ‖remainder‖, [3] ‖hi + lo‖
+    const double split = c[1] * r[1] + c[3] * r[2] + c[2] * r[3] + c[2] * r[2];
+    const double acc = (double)(keff + 16) * 0x1p-21 * (c[0] * r[0] + c[1] * r[0] + c[0] * r[1]);
+    const double rnd = (double)(2 * d + 8) * 0x1p-23;
+    *delta = __double2float_ru((split + acc + rnd) * (1.0 + 1e-9));
+}
+
+namespace {
+struct RmLayout {
+    void *opa, *opb;
+    double* pnorm;
+    unsigned long long* colmax;
+    float* delta;
+};
+RmLayout rm_carve(void* ws, int ncb, int d) {
+    const Shape sh = shape_of(d);
+    const size_t rows = (size_t)(ncb + BLOCK_M - 1) / BLOCK_M * BLOCK_M;
+    char* p = static_cast<char*>(ws);
+    RmLayout L;
+    L.opa = p;
+    p += rows * (size_t)sh.kpa * 2;
+    L.opb = p;
+    p += rows * (size_t)sh.kpb * 2;
+    L.pnorm = reinterpret_cast<double*>(p);
+    p += 4 * (size_t)ncb * 8;
+    L.colmax = reinterpret_cast<unsigned long long*>(p);
+    p += 4 * 8;
+    L.delta = reinterpret_cast<float*>(p);
+    return L;
+}
+}  // namespace
+
+size_t rowmax_bytes(int ncb, int d) {
+    const Shape sh = shape_of(d);
+    const size_t rows = (size_t)(ncb + BLOCK_M - 1) / BLOCK_M * BLOCK_M;
+    return rows * (size_t)(sh.kpa + sh.kpb) * 2 + 4 * (size_t)ncb * 8 + 4 * 8 + 16 + 256;
+}
+
+bool rowmax_supported(const Plan& plan) {
+    const Shape sh = shape_of(plan.d);
+    return !plan.fp8 && sh.kpa <= 4 * KB && sh.kpb <= 4 * KB;
+}
+
+cudaError_t launch_rowmax(const Plan& plan, const float* centers_fT, int ncb, void* ws, float* rowmax,
+                          const float** delta, unsigned long long* timeout_flag, cudaStream_t st) {
+    if (!rowmax_supported(plan) || ncb < 1) return cudaErrorInvalidValue;
+    const Shape sh = shape_of(plan.d);
+    const int rows = (ncb + BLOCK_M - 1) / BLOCK_M * BLOCK_M;
+    RmLayout L = rm_carve(ws, ncb, plan.d);
+    cudaError_t e = cudaMemsetAsync(L.colmax, 0, 4 * 8, st);
+    if (e != cudaSuccess) return e;
+    // the centres in the operands' split form (the same k_split as the rows, identity order)
+    const size_t ssm = (size_t)SPLIT_ROWS * (sh.kpa / 2 + 1 + sh.kpb / 2 + 1) * 4;
+    if ((e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm)) != cudaSuccess)
+        return e;
+    k_split<<<rows / SPLIT_ROWS, SPLIT_ROWS, ssm, st>>>(centers_fT, ncb, ncb, rows, plan.d, sh.kpa, sh.kpb,
+                                                         sh.compact ? sh.k1s * 16 : 0, nullptr,
+                                                         static_cast<__nv_bfloat16*>(L.opa),
+                                                         static_cast<__nv_bfloat16*>(L.opb), L.pnorm, L.colmax);
+    note_launch();
+    k_rowmax_delta<<<1, 32, 0, st>>>(L.colmax, reinterpret_cast<const unsigned long long*>(plan.col_max), plan.d,
+                                     sh.keff, L.delta);
+    note_launch();
+    CUtensorMap mc, mq;
+    if (!make_map(&mc, L.opa, sh.kpa, rows, BLOCK_M) || !make_map(&mq, plan.ops_b, plan.kpb, plan.np, RM_N))
+        return cudaErrorInvalidValue;
+    const int nkb_c = sh.kpa / KB, nkb_q = (sh.kpb + KB - 1) / KB;
+    const size_t fixed = 1024 + (size_t)nkb_q * RM_KB_BYTES + sizeof(RmBars), per = (size_t)nkb_c * RM_KB_BYTES;
+    // two CTAs per SM (their accumulators fill the 512 TMEM columns), and never a third
+    int stages = (int)std::min<size_t>(4, (112 * 1024 - std::min<size_t>(fixed, 112 * 1024)) / per);
+    if (stages < 1) stages = 1;
+    const size_t smem = std::max<size_t>(fixed + (size_t)stages * per, 80 * 1024);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(k_block_rowmax, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
+    const int nqb = (plan.n + RM_N - 1) / RM_N;
+    k_block_rowmax<<<nqb, NTHREADS, smem, st>>>(mc, mq, plan.n, ncb, nkb_c, nkb_q, sh.ksteps, sh.k1s, stages, rowmax,
+                                                timeout_flag);
+    note_launch();
+    *delta = L.delta;
     return cudaGetLastError();
 }
 

@@ -41,5 +41,14 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
                           unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
                           cudaStream_t st, int qb0 = 0, int qb1 = -1);
 
+// Per-row block bounds for the column lists (prune.cu): for every query block Q (128 working rows)
+// and column block B with unit centre c_B (centers_fT: [d][ncb] f32), rowmax[Q·ncb + B] = the largest
+// coarse score q·c_B over the rows q of Q, on the tensor cores with the split operands of `plan`;
+// *delta (device) receives its error margin in cosine. BF16 operands only (not the split-FP8 kind).
+bool rowmax_supported(const Plan& plan);
+size_t rowmax_bytes(int ncb, int d);
+cudaError_t launch_rowmax(const Plan& plan, const float* centers_fT, int ncb, void* ws, float* rowmax,
+                          const float** delta, unsigned long long* timeout_flag, cudaStream_t st);
+
 }  // namespace tc
 }  // namespace costal

@@ -15,6 +15,12 @@
 //             with ξ = 1e-6 rad covering the f32 rounding of the normalised rows (≤ 1e-7 rad); UB is
 //             evaluated in f32 with directed roundings and margins for the f32 dot, acosf and cosf
 //             (block_ub_f32), so it stays an upper bound;
+//   row bound with M[Q][B] = the largest coarse score q·c_B over the rows q ∈ Q (tensor cores,
+//             knn_tc.cu) and its margin δ: angle(q, c_B) ≥ acos(M + δ) for every q ∈ Q, so
+//             cos(q, x) ≤ cos(max(0, acos(M + δ) − r_B − ξ)), evaluated like UB (row_ub_f32). It
+//             drops the query block's radius, which the triangle inequality charges in full
+//             although in d dimensions the rows spread mostly across the direction to c_B; the
+//             lists use the smaller of the two bounds;
 //   lists     for every Q, the column blocks with UB ≥ t_Q, sorted by UB descending (the closest
 //             blocks first, so a query's threshold rises to its final value within the first tiles),
 //             and ub_skip[Q] = the largest UB of a skipped block. A query is certified only if its
@@ -299,6 +305,16 @@ __device__ __forceinline__ float block_ub_f32(const float* cq, float rq, const f
     return fminf(1.0f, __fadd_ru(cosf(th), 1e-6f));
 }
 
+// The per-row bound in f32 from M = max over the query block's rows of the coarse q·c_B and its
+// margin δ (M + δ ≥ the largest exact cosine of a row with c_B); radii arrive rounded up to f32,
+// acosf and cosf are covered by 1e-6 on each side, subtractions round down, the last addition up.
+__device__ __forceinline__ float row_ub_f32(float m, float delta, float rb) {
+    const float c = fmaxf(-1.0f, fminf(1.0f, __fadd_ru(m, delta)));
+    const float th = __fsub_rd(__fsub_rd(__fsub_rd(acosf(c), 1e-6f), rb), (float)XI);
+    if (th <= 0.0f) return 1.0f;
+    return fminf(1.0f, __fadd_ru(cosf(th), 1e-6f));
+}
+
 // Compare-exchange of list keys (descending) at a register distance S within a thread's run.
 template <int S, int KPT>
 __device__ __forceinline__ void cx_regs(uint64_t (&v)[KPT], int base, int size) {
@@ -399,9 +415,9 @@ template <int KPT_ALL>
 __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
                   const float* __restrict__ ccenter_f, const float* __restrict__ cradius_f, int nqb, int ncb, int d,
-                  const float* __restrict__ tq, uint32_t* __restrict__ lists, float* __restrict__ list_ub,
-                  uint32_t* __restrict__ counts, float* __restrict__ ub_skip,
-                  unsigned long long* __restrict__ skipped_total) {
+                  const float* __restrict__ tq, const float* __restrict__ rowmax, const float* __restrict__ rm_delta,
+                  uint32_t* __restrict__ lists, float* __restrict__ list_ub, uint32_t* __restrict__ counts,
+                  float* __restrict__ ub_skip, unsigned long long* __restrict__ skipped_total) {
     using LS = ListShape<KPT_ALL>;
     extern __shared__ uint64_t xk[];  // [LS::N] exchange buffer
     __shared__ float cq[64];
@@ -418,13 +434,20 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
     float rq = (float)qradius[Q];
     if ((double)rq < qradius[Q]) rq = nextafterf(rq, CUDART_INF_F);
     const float t = tq ? tq[Q] : -CUDART_INF_F;
+    const float* rm = rowmax ? rowmax + (size_t)Q * ncb : nullptr;
+    const float delta = rowmax ? *rm_delta : 0.0f;
+    // the smaller of the cone bound and the per-row bound
+    auto bound = [&](int b, float* phi) {
+        const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d, phi);
+        return rm ? fminf(u, row_ub_f32(rm[b], delta, cradius_f[b])) : u;
+    };
     uint32_t* out = lists + (size_t)Q * ncb;
     float* out_ub = list_ub + (size_t)Q * ncb;
     if (ncb > LS::N) {
         if (tid == 0) {
             unsigned c = 0;
             for (int b = 0; b < ncb; ++b) {
-                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d);
+                const float u = bound(b, nullptr);
                 if (u >= t) {
                     out_ub[c] = CUDART_INF_F;  // block order: the bounds do not decrease along the list
                     out[c++] = (uint32_t)b;
@@ -447,7 +470,7 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
             v[j] = 0ull;  // absent or skipped: sorts last
             if (b < ncb) {
                 float phi;
-                const float u = block_ub_f32(cq, rq, ccenter_f + b, ncb, cradius_f[b], d, &phi);
+                const float u = bound(b, &phi);
                 if (u >= t) {
                     ++my_kept;
                     // the bound (possibly negative) as an order-preserving u32 above the complemented id
@@ -685,8 +708,9 @@ cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t
     const size_t smem = (size_t)(wide ? ListShape<32>::N : ListShape<16>::N) * 8;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq, P.lists,
-                                      P.list_ub, P.counts, P.ub_skip, skipped_total); note_launch();
+    kern<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq,
+                                      P.rowmax, P.rm_delta, P.lists, P.list_ub, P.counts, P.ub_skip, skipped_total);
+    note_launch();
     k_row_ub<<<(P.n + 255) / 256, 256, 0, st>>>(P.perm, P.n, P.ub_skip, P.row_ub); note_launch();
     return cudaGetLastError();
 }

@@ -205,6 +205,13 @@ int costal_mlp_forward(const float* params, uint32_t F, const float* feat, uint6
                        size_t errlen);
 int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, const float* y, uint64_t m,
                         float quantile, float* grad, char* err, size_t errlen);
+/* Test hook: the per-row block bound data of the tensor-core path for X (host, n x d, 1 <= d <= 64):
+ * the working order perm[n] (working -> original row), the column blocks' unit centres ccenter[ncb][d]
+ * and angular radii cradius[ncb] (f64, blocks of 256 working rows), rowmax[nqb][ncb] = the largest
+ * split-BF16 coarse score of a query block's rows (blocks of 128) with each centre, and *delta, its
+ * error margin in cosine; nqb = ceil(n/128), ncb = ceil(n/256). */
+int costal_block_bounds(const float* x, uint64_t n, uint32_t d, uint32_t* perm, double* ccenter, double* cradius,
+                        float* rowmax, float* delta, char* err, size_t errlen);
 
 /* ---- the host consumer: Leiden (leiden="fast"), crates/costal-core/src/leiden.rs ------------- */
 /* lib.rs:275-306 `_leiden` (from_coo = 0, objective = 0) and lib.rs:356-412 `_leiden_coo`
