@@ -465,12 +465,13 @@ def main():
         torch.cuda.synchronize()
         step_host()
     e2e_t = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        step_host()
-        e2e_t.append(time.perf_counter() - t)
+    with ClockSampler(local) as e2e_clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            step_host()
+            e2e_t.append(time.perf_counter() - t)
     e2e_s = max_over_ranks(float(np.mean(e2e_t)), "cuda")
     # parity guard: the timed host result equals the device-resident one
     assert int(m2.value) == edges
@@ -565,7 +566,9 @@ def main():
             "config": {"workload": wl.name, "n": n, "d": d, "k": k, "margin": wl.margin, "backend": args.backend,
                        "learned_prune": learned, "weight": "tanimoto",
                        "l2": "flushed between steps (512 MB write outside the timed events)"},
-            "e2e": {"value": job_cells_per_s(n, 1, e2e_s * 1e3), "unit": "cells/s", "h2d_bytes_per_step": n * d * 4 * ws,
+            "e2e": {"value": job_cells_per_s(n, 1, e2e_s * 1e3), "unit": "cells/s", "ms_per_step": e2e_s * 1e3,
+                    "ms_steps": [round(t_ * 1e3, 2) for t_ in e2e_t], "clocks": e2e_clocks.summary(),
+                    "h2d_bytes_per_step": n * d * 4 * ws,
                     "d2h_bytes_per_step": edges * 16},
             "gpu_launches": int(launches),
             "gpu_launches_per_step": launches / args.steps,

@@ -203,18 +203,18 @@ __global__ void k_cell_scatter(const uint32_t* __restrict__ cell, int n, int K, 
 
 // ---- block geometry -------------------------------------------------------------------------------
 
-// One CTA per block of `bs` consecutive working rows: centre = normalised f64 sum (row order),
-// radius = the largest angle between a row and the centre (f64). Rows past n are ignored.
-__global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const uint32_t* __restrict__ perm, int n,
-                             int bs, double* __restrict__ center, double* __restrict__ radius,
-                             float* __restrict__ center_f, float* __restrict__ radius_f) {
+// One CTA per block of `bs` consecutive working rows (wrows: the normalised rows in working order,
+// row-major [n][d]): centre = normalised f64 sum (row order), radius = the largest angle between a row
+// and the centre (f64). Rows past n are ignored.
+__global__ void k_block_geom(const float* __restrict__ wrows, int d, int n, int bs, double* __restrict__ center,
+                             double* __restrict__ radius, float* __restrict__ center_f, float* __restrict__ radius_f) {
     __shared__ double c_s[64];
     __shared__ double red[256];
     const int b = blockIdx.x;
     const int r0 = b * bs, r1 = min(n, r0 + bs);
     if (threadIdx.x < d) {
         double s = 0.0;
-        for (int w = r0; w < r1; ++w) s += (double)xsT[(size_t)threadIdx.x * np + perm[w]];
+        for (int w = r0; w < r1; ++w) s += (double)wrows[(size_t)w * d + threadIdx.x];
         c_s[threadIdx.x] = s;
     }
     __syncthreads();
@@ -240,10 +240,10 @@ __global__ void k_block_geom(const float* __restrict__ xsT, int np, int d, const
     const float margin = (float)(2 * d + 8) * 0x1p-23f;
     float worst = 0.0f;
     for (int w = r0 + threadIdx.x; w < r1; w += blockDim.x) {
-        const uint32_t o = perm[w];
+        const float* row = wrows + (size_t)w * d;
         float dot = 0.0f, nn = 0.0f;
         for (int t = 0; t < d; ++t) {
-            const float v = xsT[(size_t)t * np + o];
+            const float v = row[t];
             dot = fmaf(v, cf_s[t], dot);
             nn = fmaf(v, v, nn);
         }
@@ -276,15 +276,46 @@ constexpr int LIST_T = 512;
 constexpr double XI = 1e-6;
 
 // A list sort's shape: KPT keys per thread over LIST_T threads (16 → 8,192 column blocks, two CTAs
-// per SM; 32 → 16,384, one CTA per SM with the keys in its registers). The low key word packs the
-// centre angle above the complemented block id: ID_BITS bits of id, 32 − ID_BITS of angle.
+// per SM; 32 → 16,384, one CTA per SM with the keys in its registers). A key is 32 bits: a level of
+// SBITS = 32 − ID_BITS bits above the complemented block id (ID_BITS bits). Levels [1, ONE) hold a
+// bound u < 1 rounded up to a multiple of Q = 2 / ONE (u ≤ level·Q − 1 + Q); levels [ONE, 2·ONE) hold
+// the blocks whose bound is 1, nearest centre first. Descending keys: larger bound first, then (at
+// bound 1) smaller centre angle, then smaller block id.
 template <int KPT>
 struct ListShape {
     static constexpr int N = LIST_T * KPT;
     static constexpr int ID_BITS = KPT <= 16 ? 13 : 14;
     static constexpr uint32_t ID_MAX = (1u << ID_BITS) - 1u;
-    static constexpr uint32_t PHI_MAX = (1u << (32 - ID_BITS)) - 1u;
+    static constexpr int SBITS = 32 - ID_BITS;
+    static constexpr uint32_t ONE = 1u << (SBITS - 1);     // first level of the bound-1 range
+    static constexpr float SCALE = (float)(1u << (SBITS - 2));  // levels per unit of (u + 1)
 };
+
+// The key of column block b with bound u (≤ 1) and centre angle φ (0 for a padding key never occurs:
+// every key of a kept block is non-zero).
+template <int KPT>
+__device__ __forceinline__ uint32_t list_key(float u, float phi, int b) {
+    using LS = ListShape<KPT>;
+    uint32_t level;
+    if (u >= 1.0f) {
+        const float q = fmaxf(0.0f, phi) * ((float)LS::ONE / 3.14159265f);
+        level = (2u * LS::ONE - 1u) - (uint32_t)fminf((float)(LS::ONE - 1u), q);
+    } else {
+        // ⌊(u + 1)·SCALE⌋ with u + 1 rounded up: level·Q − 1 + Q ≥ u holds for the level kept
+        const float f = floorf(__fadd_ru(fmaxf(u, -1.0f), 1.0f) * LS::SCALE);
+        level = (uint32_t)fminf((float)(LS::ONE - 1u), fmaxf(1.0f, f));
+    }
+    return (level << LS::ID_BITS) | (LS::ID_MAX - (uint32_t)b);
+}
+
+// The bound a key stands for: 1 in the bound-1 range, else the top of its level (exact in f32).
+template <int KPT>
+__device__ __forceinline__ float key_bound(uint32_t key) {
+    using LS = ListShape<KPT>;
+    const uint32_t level = key >> LS::ID_BITS;
+    if (level >= LS::ONE) return 1.0f;
+    return (float)(level + 1u) * (1.0f / LS::SCALE) - 1.0f;
+}
 
 // The bound in f32 for one (query block, column block) pair, rigorous for the f64 geometry: the
 // f32 FMA dot of the two unit centres (each rounded to f32) is within (d + 2)·2⁻²⁴ of the f64 value,
@@ -317,14 +348,14 @@ __device__ __forceinline__ float row_ub_f32(float m, float delta, float rb) {
 
 // Compare-exchange of list keys (descending) at a register distance S within a thread's run.
 template <int S, int KPT>
-__device__ __forceinline__ void cx_regs(uint64_t (&v)[KPT], int base, int size) {
+__device__ __forceinline__ void cx_regs(uint32_t (&v)[KPT], int base, int size) {
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         const int p = j ^ S;
         if (p > j) {
             const bool desc = ((base + j) & size) == 0;
-            const uint64_t a = v[j], b = v[p];
-            const uint64_t hi = a > b ? a : b, lo = a > b ? b : a;
+            const uint32_t a = v[j], b = v[p];
+            const uint32_t hi = max(a, b), lo = min(a, b);
             v[j] = desc ? hi : lo;
             v[p] = desc ? lo : hi;
         }
@@ -334,7 +365,7 @@ __device__ __forceinline__ void cx_regs(uint64_t (&v)[KPT], int base, int size) 
 // Bitonic sort (descending) of the CTA's LIST_T·KPT keys, KPT per thread at positions base..base+KPT−1:
 // compare-exchanges in registers, by warp shuffles, or through shared memory (xk) by distance.
 template <int KPT>
-__device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk, int base, int lane) {
+__device__ __forceinline__ void block_sort_keys(uint32_t (&v)[KPT], uint32_t* xk, int base, int lane) {
     constexpr int N = LIST_T * KPT;
     for (int size = 2; size <= N; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -346,9 +377,9 @@ __device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk
 #pragma unroll
                 for (int j = 0; j < KPT; ++j) {
                     const int e = base + j;
-                    const uint64_t o = xk[e ^ stride];
+                    const uint32_t o = xk[e ^ stride];
                     const bool keep_max = ((e & stride) == 0) == ((e & size) == 0);
-                    const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                    const uint32_t hi = max(v[j], o), lo = min(v[j], o);
                     v[j] = keep_max ? hi : lo;
                 }
             } else if (stride >= KPT) {  // within the warp
@@ -356,9 +387,9 @@ __device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk
 #pragma unroll
                 for (int j = 0; j < KPT; ++j) {
                     const int e = base + j;
-                    const uint64_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[j], lstride);
+                    const uint32_t o = __shfl_xor_sync(COSTAL_FULL_MASK, v[j], lstride);
                     const bool keep_max = ((lane & lstride) == 0) == ((e & size) == 0);
-                    const uint64_t hi = v[j] > o ? v[j] : o, lo = v[j] > o ? o : v[j];
+                    const uint32_t hi = max(v[j], o), lo = min(v[j], o);
                     v[j] = keep_max ? hi : lo;
                 }
             } else if (stride == 16) {
@@ -376,17 +407,17 @@ __device__ __forceinline__ void block_sort_keys(uint64_t (&v)[KPT], uint64_t* xk
     }
 }
 
-// The sorted keys out: list position e holds block ID_MAX − (low ID_BITS bits) and its bound.
-template <int KPT, int ID_BITS>
-__device__ __forceinline__ void write_keys(const uint64_t (&v)[KPT], int base, unsigned nk, uint32_t* out, float* out_ub) {
-    constexpr uint32_t ID_MAX = (1u << ID_BITS) - 1u;
+// The sorted keys out (keys of ListShape<KPT_ALL>, KPT per thread): list position e holds block
+// ID_MAX − (low ID_BITS bits) and the bound its level stands for.
+template <int KPT, int KPT_ALL>
+__device__ __forceinline__ void write_keys(const uint32_t (&v)[KPT], int base, unsigned nk, uint32_t* out, float* out_ub) {
+    using LS = ListShape<KPT_ALL>;
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         const unsigned e = (unsigned)(base + j);
         if (e < nk) {
-            const uint32_t hk = (uint32_t)(v[j] >> 32);
-            out[e] = ID_MAX - ((uint32_t)v[j] & ID_MAX);
-            out_ub[e] = __uint_as_float((hk & 0x80000000u) ? (hk & 0x7fffffffu) : ~hk);
+            out[e] = LS::ID_MAX - (v[j] & LS::ID_MAX);
+            out_ub[e] = key_bound<KPT_ALL>(v[j]);
         }
     }
 }
@@ -394,10 +425,10 @@ __device__ __forceinline__ void write_keys(const uint64_t (&v)[KPT], int base, u
 // Compact the kept keys (non-zero) of every thread into xk[0 .. kept) in any order, zero-fill up to
 // LIST_T·KPT, and load KPT of them per thread.
 template <int KPT, int KPT_ALL>
-__device__ __forceinline__ void compact_keys(const uint64_t (&all)[KPT_ALL], uint64_t (&v)[KPT], uint64_t* xk,
+__device__ __forceinline__ void compact_keys(const uint32_t (&all)[KPT_ALL], uint32_t (&v)[KPT], uint32_t* xk,
                                              unsigned* slot, unsigned nk, int base) {
     constexpr int N = LIST_T * KPT;
-    for (int e = threadIdx.x + (int)nk; e < N; e += LIST_T) xk[e] = 0ull;
+    for (int e = threadIdx.x + (int)nk; e < N; e += LIST_T) xk[e] = 0u;
 #pragma unroll
     for (int j = 0; j < KPT_ALL; ++j)
         if (all[j]) xk[atomicAdd(slot, 1u)] = all[j];
@@ -408,9 +439,10 @@ __device__ __forceinline__ void compact_keys(const uint64_t (&all)[KPT_ALL], uin
 }
 
 // One CTA per query block: the upper bound against every column block; the blocks kept (UB ≥ t_Q)
-// sorted by (UB desc, centre angle asc, block asc) with their bounds — a bitonic sort of 64-bit keys, 16 per thread,
-// exchanged in registers, by warp shuffles or through shared memory by distance — and the largest UB
-// of a skipped block. Lists longer than the shape's N stay in block order with bounds +inf.
+// sorted by (UB desc, centre angle asc at UB = 1, block asc) with their bounds rounded up to the keys'
+// levels — a bitonic sort of 32-bit keys, 16 per thread, exchanged in registers, by warp shuffles or
+// through shared memory by distance — and the largest UB of a skipped block. Lists longer than the
+// shape's N stay in block order with bounds +inf.
 template <int KPT_ALL>
 __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
     k_block_lists(const double* __restrict__ qcenter, const double* __restrict__ qradius,
@@ -419,7 +451,7 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
                   uint32_t* __restrict__ lists, float* __restrict__ list_ub, uint32_t* __restrict__ counts,
                   float* __restrict__ ub_skip, unsigned long long* __restrict__ skipped_total) {
     using LS = ListShape<KPT_ALL>;
-    extern __shared__ uint64_t xk[];  // [LS::N] exchange buffer
+    extern __shared__ uint32_t xk[];  // [LS::N] exchange buffer
     __shared__ float cq[64];
     __shared__ unsigned kept, slot;
     __shared__ int skip_max_bits;
@@ -459,7 +491,7 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
         }
     } else {
         const int base = tid * KPT_ALL;
-        uint64_t v[KPT_ALL];
+        uint32_t v[KPT_ALL];
         unsigned my_kept = 0;
         int my_skip = __float_as_int(-CUDART_INF_F);
         // keys are computed for blocks j·LIST_T + tid (coalesced reads of the transposed centres); the
@@ -467,21 +499,15 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
 #pragma unroll
         for (int j = 0; j < KPT_ALL; ++j) {
             const int b = j * LIST_T + tid;
-            v[j] = 0ull;  // absent or skipped: sorts last
+            v[j] = 0u;  // absent or skipped: sorts last
             if (b < ncb) {
                 float phi;
                 const float u = bound(b, &phi);
                 if (u >= t) {
                     ++my_kept;
-                    // the bound (possibly negative) as an order-preserving u32 above the complemented id
-                    const uint32_t ub = __float_as_uint(u);
-                    const uint32_t hk = (ub & 0x80000000u) ? ~ub : (ub | 0x80000000u);
-                    // ties of the bound (e.g. every block of the query's own cluster at 1) go nearest
-                    // centre first, then by block: the low word is (PHI_MAX − φ quantised) · 2^ID_BITS + (ID_MAX − b)
-                    const uint32_t qphi = (uint32_t)fminf((float)LS::PHI_MAX,
-                                                          fmaxf(0.0f, phi) * ((float)(LS::PHI_MAX + 1u) / 3.14159265f));
-                    const uint32_t lo = ((LS::PHI_MAX - qphi) << LS::ID_BITS) | (LS::ID_MAX - (uint32_t)b);
-                    v[j] = ((uint64_t)hk << 32) | (uint64_t)lo;
+                    // ties of the bound at 1 (e.g. every block of the query's own cluster) go nearest
+                    // centre first, then by block
+                    v[j] = list_key<KPT_ALL>(u, phi, b);
                 } else {
                     // a skipped block's bound, clamped at 0 so that the int order of the bits is the float order
                     my_skip = max(my_skip, __float_as_int(fmaxf(u, 0.0f)));
@@ -493,26 +519,25 @@ __global__ void __launch_bounds__(LIST_T, KPT_ALL <= 16 ? 2 : 1)
         __syncthreads();  // kept is final
         const unsigned nk = kept;
         // Short lists (a learned threshold skips most blocks) sort only their kept keys, compacted.
-        constexpr int IB = LS::ID_BITS;
         if (nk <= (unsigned)(LIST_T * 4)) {
-            uint64_t w[4];
+            uint32_t w[4];
             compact_keys<4>(v, w, xk, &slot, nk, tid * 4);
             block_sort_keys<4>(w, xk, tid * 4, lane);
-            write_keys<4, IB>(w, tid * 4, nk, out, out_ub);
+            write_keys<4, KPT_ALL>(w, tid * 4, nk, out, out_ub);
         } else if (nk <= (unsigned)(LIST_T * 8)) {
-            uint64_t w[8];
+            uint32_t w[8];
             compact_keys<8>(v, w, xk, &slot, nk, tid * 8);
             block_sort_keys<8>(w, xk, tid * 8, lane);
-            write_keys<8, IB>(w, tid * 8, nk, out, out_ub);
+            write_keys<8, KPT_ALL>(w, tid * 8, nk, out, out_ub);
         } else if (KPT_ALL > 16 && nk <= (unsigned)(LIST_T * 16)) {
-            uint64_t w[16];
+            uint32_t w[16];
             compact_keys<16>(v, w, xk, &slot, nk, tid * 16);
             block_sort_keys<16>(w, xk, tid * 16, lane);
-            write_keys<16, IB>(w, tid * 16, nk, out, out_ub);
+            write_keys<16, KPT_ALL>(w, tid * 16, nk, out, out_ub);
         } else {
             // the keys start interleaved over all N positions, so the sort covers all of them
             block_sort_keys<KPT_ALL>(v, xk, base, lane);
-            write_keys<KPT_ALL, IB>(v, base, nk, out, out_ub);
+            write_keys<KPT_ALL, KPT_ALL>(v, base, nk, out, out_ub);
         }
     }
     __syncthreads();
@@ -550,7 +575,7 @@ size_t workspace_bytes(int n, int d) {
     return a256(n * 4ull) * 2 + a256((size_t)K_CENTROIDS * d * 4) + a256(nqb * d * 8) + a256(nqb * 8) +
            a256(ncb * d * 8) + a256(ncb * 8) + a256(ncb * d * 4) + a256(ncb * 4) + 2 * a256(nqb * ncb * 4) +
            a256(nqb * 4) + a256(nqb * 4) + a256(n * 8ull) + a256(nqb * 4) + a256(m * d * 4) + a256(m * 4) + a256(nch * K_CENTROIDS * 4) + a256((K_CENTROIDS + 1) * 4) +
-           a256(m * 4) + 4096;
+           a256(m * 4) + a256((size_t)n * d * 4) + 4096;
 }
 
 namespace {
@@ -560,6 +585,7 @@ struct Scratch {
     uint32_t* hist;
     uint32_t* cell_start;
     uint32_t* sample_idx;
+    float* wrows;  // [n][d] the normalised rows in working order
 };
 
 __global__ void k_sample_idx(uint32_t* idx, int m, int n) {
@@ -613,6 +639,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     S.hist = reinterpret_cast<uint32_t*>(take((size_t)nch * K * 4));
     S.cell_start = reinterpret_cast<uint32_t*>(take((size_t)(K + 1) * 4));
     S.sample_idx = reinterpret_cast<uint32_t*>(take((size_t)m * 4));
+    S.wrows = reinterpret_cast<float*>(take((size_t)n * d * 4));
     P.scratch = S.sample_rows;
 
     const size_t csm = (size_t)K * ((d + 3) & ~3) * 4;
@@ -630,9 +657,10 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     k_cell_hist<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist); note_launch();
     k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start); note_launch();
     k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm); note_launch();
-    k_block_geom<<<nqb, 256, 0, st>>>(xsT, np, d, P.perm, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
-    k_block_geom<<<ncb, 256, 0, st>>>(xsT, np, d, P.perm, n, CB, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f);
-    note_launch();
+    // the rows in working order, row-major, for the block geometry's contiguous reads
+    k_gather_rows<<<std::min((n * d + 255) / 256, 8 * 1024), 256, 0, st>>>(xsT, np, d, P.perm, n, S.wrows); note_launch();
+    k_block_geom<<<nqb, 256, 0, st>>>(S.wrows, d, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
+    k_block_geom<<<ncb, 256, 0, st>>>(S.wrows, d, n, CB, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f); note_launch();
     return cudaGetLastError();
 }
 
@@ -705,7 +733,7 @@ cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t
     // (n ≤ 4,194,304): 32 keys a thread; beyond that the lists stay in block order (no early stop)
     const bool wide = P.ncb > ListShape<16>::N;
     auto kern = wide ? k_block_lists<32> : k_block_lists<16>;
-    const size_t smem = (size_t)(wide ? ListShape<32>::N : ListShape<16>::N) * 8;
+    const size_t smem = (size_t)(wide ? ListShape<32>::N : ListShape<16>::N) * 4;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<P.nqb, LIST_T, smem, st>>>(P.qcenter, P.qradius, P.ccenter_f, P.cradius_f, P.nqb, P.ncb, P.d, P.tq,
