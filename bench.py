@@ -444,6 +444,7 @@ def main():
     h_cols = torch.empty(n * k, dtype=torch.int32, pin_memory=True)
     h_w = torch.empty(n * k, dtype=torch.float64, pin_memory=True)
     m2 = C.c_uint64()
+    st_host = L.KnnStats()  # the kNN stage's device time inside the host call
 
     def step_host():
         if sharded:  # X from pinned host memory to this rank's GPU, the sharded step, the edges back
@@ -457,14 +458,15 @@ def main():
             return
         rc = lib.costal_build_graph(C.c_void_p(hx.data_ptr()), n, d, k, C.byref(opts), weight,
                                     C.c_void_p(h_rows.data_ptr()), C.c_void_p(h_cols.data_ptr()),
-                                    C.c_void_p(h_w.data_ptr()), C.byref(m2), None, None, None, None, err, errlen)
+                                    C.c_void_p(h_w.data_ptr()), C.byref(m2), None, None, None, C.byref(st_host), err,
+                                    errlen)
         L.check(rc, err)
 
     for _ in range(args.warmup):
         flush.zero_()
         torch.cuda.synchronize()
         step_host()
-    e2e_t = []
+    e2e_t, e2e_knn = [], []
     with ClockSampler(local) as e2e_clocks:
         for _ in range(args.steps):
             flush.zero_()
@@ -472,6 +474,8 @@ def main():
             t = time.perf_counter()
             step_host()
             e2e_t.append(time.perf_counter() - t)
+            if not sharded:
+                e2e_knn.append(st_host.ms_total)
     e2e_s = max_over_ranks(float(np.mean(e2e_t)), "cuda")
     # parity guard: the timed host result equals the device-resident one
     assert int(m2.value) == edges
@@ -567,7 +571,8 @@ def main():
                        "learned_prune": learned, "weight": "tanimoto",
                        "l2": "flushed between steps (512 MB write outside the timed events)"},
             "e2e": {"value": job_cells_per_s(n, 1, e2e_s * 1e3), "unit": "cells/s", "ms_per_step": e2e_s * 1e3,
-                    "ms_steps": [round(t_ * 1e3, 2) for t_ in e2e_t], "clocks": e2e_clocks.summary(),
+                    "ms_steps": [round(t_ * 1e3, 2) for t_ in e2e_t],
+                    "ms_knn_device": float(np.mean(e2e_knn)) if e2e_knn else None, "clocks": e2e_clocks.summary(),
                     "h2d_bytes_per_step": n * d * 4 * ws,
                     "d2h_bytes_per_step": edges * 16},
             "gpu_launches": int(launches),

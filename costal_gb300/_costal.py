@@ -452,17 +452,23 @@ def _mlp_forward(params, feat):
     return out
 
 
+def col_block_rows(n):
+    """Rows of a column block of the tensor-core path's lists for n rows (prune.h col_block)."""
+    return 128 if (n + 127) // 128 <= 8192 else 256
+
+
 def _block_bounds(x):
     """Test hook: the tensor-core path's per-row block bound data for X (n, d), d <= 64.
 
     Returns (perm, ccenter, cradius, rowmax, delta): the working order (working -> original row),
-    the unit centres (ncb, d) and angular radii (ncb,) of the column blocks of 256 working rows, the
-    largest split-BF16 coarse score of each query block's rows (blocks of 128) with each centre
-    (nqb, ncb), and that score's error margin in cosine.
+    the unit centres (ncb, d) and angular radii (ncb,) of the column blocks (128 working rows while
+    ceil(n / 128) <= 8,192, else 256), the largest split-BF16 coarse score of each query block's rows
+    (blocks of 128) with each centre (nqb, ncb), and that score's error margin in cosine.
     """
     x = np.ascontiguousarray(x, dtype=np.float32)
     n, d = x.shape
-    nqb, ncb = (n + 127) // 128, (n + 255) // 256
+    cb = col_block_rows(n)
+    nqb, ncb = (n + 127) // 128, (n + cb - 1) // cb
     perm = np.empty(n, np.uint32)
     ccenter = np.empty((ncb, d), np.float64)
     cradius = np.empty(ncb, np.float64)

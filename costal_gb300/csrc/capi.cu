@@ -257,6 +257,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     CK(cudaEventRecord(c.ev[5], s));
     const bool tanimoto = o.select == COSTAL_SELECT_TANIMOTO;
     bool used_tc = false;
+    int list_cb = 0;  // rows of a column block of the tensor-core path's lists (0: no lists)
     // The split-FP8 kind: its coarse scores are ~2⁻⁸ coarser than split BF16's, so it keeps 64
     // candidates a row whatever the margin (the output does not depend on it) to let the certificate
     // hold for nearly every row.
@@ -355,6 +356,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
                     pp.tq = nullptr;
                 }
                 CK(prune::build_lists(pp, &dm->blocks_skipped, s));
+                list_cb = pp.cb;
             }
             if (shard && nrows > 0) {  // the shard's rows: its query blocks in the processing order
                 if (ordered)
@@ -368,7 +370,8 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             if (nrows > 0)
                 CK(tc::launch_coarse(plan, cap, ordered ? pp.lists : nullptr,
                                      ordered && o.prune ? pp.list_ub : nullptr, ordered ? pp.counts : nullptr,
-                                     ordered ? pp.ncb : 0, c.cand_idx.as<uint32_t>(), c.cand_score.as<float>(),
+                                     ordered ? pp.ncb : 0, ordered ? pp.cb : 0, c.cand_idx.as<uint32_t>(),
+                                     c.cand_score.as<float>(),
                                      c.tau.as<float>(), &dm->blocks_stopped, &dm->timeout_flag, c.sm_count, s, qb0,
                                      qb1));
             CK(cudaEventRecord(c.ev[2], s));
@@ -448,7 +451,7 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
     if (st) {
         st->fallback_rows = hm.fb_count;
         st->row_block = 128;
-        st->col_block = used_tc ? (uint64_t)tc::BLOCK_N : 128;
+        st->col_block = used_tc ? (uint64_t)(list_cb ? list_cb : tc::BLOCK_N) : 128;
         st->blocks_skipped = hm.blocks_skipped;
         st->blocks_stopped = hm.blocks_stopped;
         st->blocks_total = (uint64_t)(qb1 - qb0) * (uint64_t)((n + st->col_block - 1) / st->col_block);

@@ -54,6 +54,8 @@ namespace tc {
 constexpr int KB = 64;                 // bf16 elements per 128-byte swizzle row (one K block)
 constexpr int A_KB_BYTES = BLOCK_M * 128;  // 16 KB per K block of the query tile
 constexpr int B_KB_BYTES = BLOCK_N * 128;  // 32 KB per K block of a column tile
+constexpr int HALF_N = BLOCK_N / 2;            // columns of one TMA box of a column tile
+constexpr int B_HALF_BYTES = HALF_N * 128;     // 16 KB: the second half of a K block
 constexpr int EPI_WARPS = 4;
 constexpr int NTHREADS = (EPI_WARPS + 2) * 32;  // 4 epilogue warps, 1 TMA warp, 1 MMA warp
 constexpr uint32_t TMEM_COLS = 512;    // two 256-column FP32 accumulators
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
                 int nkb, int nkb_b, int ksteps, int k1s, int stages, int cap, const uint32_t* __restrict__ perm,
                 const uint32_t* __restrict__ lists, const float* __restrict__ list_ub,
-                const uint32_t* __restrict__ counts, int ncb, const double* __restrict__ row_eps,
+                const uint32_t* __restrict__ counts, int ncb, int epc, const double* __restrict__ row_eps,
                 uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
                 unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag,
                 int qb0) {
@@ -433,9 +435,36 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // CTA b takes query block qb0 + b (a launch over a contiguous range of query blocks: one shard).
     const int qb = qb0 + (int)blockIdx.x;
     const int q0 = qb * BLOCK_M;
-    const int ntiles = lists ? (int)counts[qb] : np / BLOCK_N;
+    // A tile's 256 columns are two halves of HALF_N, each loaded by its own TMA box: with lists of
+    // 128-column blocks (epc = 2) two consecutive list entries, with lists of 256-column blocks (epc =
+    // 1) one entry, without lists 256 consecutive columns. An odd list's last tile has one entry; its
+    // second half repeats the first and the epilogue leaves it out.
+    const int nentries = lists ? (int)counts[qb] : 0;
+    const int ntiles = lists ? (nentries + epc - 1) / epc : np / BLOCK_N;
     const uint32_t* my_list = lists ? lists + (size_t)qb * ncb : nullptr;
-    auto block_of = [&](int t) -> int { return my_list ? (int)my_list[t] : t; };
+    auto tile_cols = [&](int t, int& c0, int& c1) -> bool {
+        if (!my_list) {
+            c0 = t * BLOCK_N;
+            c1 = c0 + HALF_N;
+            return true;
+        }
+        if (epc == 1) {
+            c0 = (int)my_list[t] * BLOCK_N;
+            c1 = c0 + HALF_N;
+            return true;
+        }
+        const bool two = 2 * t + 1 < nentries;
+        c0 = (int)my_list[2 * t] * HALF_N;
+        c1 = two ? (int)my_list[2 * t + 1] * HALF_N : c0;
+        return two;
+    };
+    // the list entries of tile t lie inside the operands (the list kernel never writes others)
+    auto tile_ok = [&](int t) -> bool {
+        if (!my_list) return true;
+        const unsigned lim = (unsigned)(np / (epc == 1 ? BLOCK_N : HALF_N));
+        if (epc == 1) return my_list[t] < lim;
+        return my_list[2 * t] < lim && (2 * t + 1 >= nentries || my_list[2 * t + 1] < lim);
+    };
     const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb_b * B_KB_BYTES;
     (void)a_bytes;
 
@@ -470,7 +499,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const float* my_ub = list_ub ? list_ub + (size_t)qb * ncb : nullptr;
             bool go = true;
             for (int t = 0; go && t < ntiles; ++t) {
-                const int cb = block_of(t) * BLOCK_N;
+                const bool ok = tile_ok(t);
+                int c0 = 0, c1 = 0;
+                if (ok) tile_cols(t, c0, c1);
                 for (int kb = 0; kb < nkb; ++kb) {
                     const int g = t * nkb + kb, s = g % stages;
                     const uint32_t ph = (uint32_t)(g / stages) & 1u;
@@ -480,15 +511,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                     if (kb == 0) {
                         bool stop = false;
-                        if ((unsigned)block_of(t) >= (unsigned)(np / BLOCK_N)) {
+                        if (!ok) {
                             atomicExch(timeout_flag, 2ull);  // never produced by the list kernel
                             stop = true;
                         } else if (t > 0 && my_ub) {
                             volatile float* wf = bars->warp_floor;
                             const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
-                            if (my_ub[t] < fl) {
+                            if (my_ub[t * epc] < fl) {
                                 stop = true;
-                                if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
+                                if (stopped_total)
+                                    atomicAdd(stopped_total, (unsigned long long)(nentries - t * epc));
                             }
                         }
                         if (stop) {
@@ -501,7 +533,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     mbar_expect_tx(&bars->b_full[s], (uint32_t)(A_KB_BYTES + B_KB_BYTES));
                     unsigned char* dst = b_tiles + (size_t)s * stage_bytes;
                     tma_load_2d(dst, &map_a, kb * KBE, q0, &bars->b_full[s]);
-                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KBE, cb, &bars->b_full[s]);
+                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
+                    tma_load_2d(dst + A_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
                 }
             }
         }
@@ -513,7 +546,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int s = t % stages;
                 const uint32_t ph = (uint32_t)(t / stages) & 1u;
                 if (!mbar_wait(&bars->b_empty[s], ph ^ 1u, timeout_flag, true)) break;
-                if ((unsigned)block_of(t) >= (unsigned)(np / BLOCK_N)) {
+                if (!tile_ok(t)) {
                     // a list entry outside the operands (never produced by the list kernel): report it
                     // and stop the CTA here like an early stop, so no role reads past the operands
                     atomicExch(timeout_flag, 2ull);
@@ -522,26 +555,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     break;
                 }
                 if (t > 0 && my_ub) {
-                    // Every column of list entry t (and of all later ones: the bounds do not increase)
-                    // has cosine ≤ my_ub[t]; its coarse score is ≤ my_ub[t] + E_i. When that is below
-                    // every row's threshold τ_i, none of them can be admitted: stop here. The floors
-                    // read may be stale, i.e. lower, which only delays the stop.
+                    // Every column of the tile's first list entry (and of all later ones: the bounds do
+                    // not increase) has cosine ≤ its bound; its coarse score is ≤ bound + E_i. When that
+                    // is below every row's threshold τ_i, none of them can be admitted: stop here. The
+                    // floors read may be stale, i.e. lower, which only delays the stop.
                     volatile float* wf = bars->warp_floor;
                     const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
-                    if (my_ub[t] < fl) {
+                    if (my_ub[t * epc] < fl) {
                         *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
-                        if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(ntiles - t));
+                        if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(nentries - t * epc));
                         mbar_arrive(&bars->b_full[s]);  // completes the phase without data (release)
                         break;
                     }
                 }
                 mbar_expect_tx(&bars->b_full[s], b_bytes);
                 unsigned char* dst = b_tiles + (size_t)s * b_bytes;
-                const int cb = block_of(t) * BLOCK_N;
+                int c0, c1;
+                tile_cols(t, c0, c1);
                 // (the last K block may reach past the operand's row: TMA fills those columns with zeros
                 // and reads nothing for them)
-                for (int kb = 0; kb < nkb_b; ++kb)
-                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KBE, cb, &bars->b_full[s]);
+                for (int kb = 0; kb < nkb_b; ++kb) {
+                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
+                    tma_load_2d(dst + kb * B_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
+                }
             }
         }
     } else if (warp == EPI_WARPS + 1) {
@@ -627,7 +663,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (!mbar_wait(&bars->t_full[buf], bph, timeout_flag, false)) break;
             tc_fence_after();
             if (*reinterpret_cast<volatile int*>(&bars->stop_tile) == t) break;
-            const int c0 = block_of(t) * BLOCK_N;
+            int c0, c1;
+            const bool two = tile_cols(t, c0, c1);  // false: the tile's second half has no list entry
             const uint32_t tb = lane_addr + (uint32_t)(buf * BLOCK_N);
             if (t == 0) {
                 // A starting threshold from the first tiles: the cap-th largest of their column-group
@@ -636,19 +673,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 // be among the query's best cap. (When the
                 // query's own column or padding supplies one of those maxima, τ₀ can be a little too
                 // high; that only costs the certificate, since τ never falls and everything left out
-                // stays below it.) The first tile itself is admitted at ≥ τ₀ (one below in the strict
-                // test), later tiles at > τ as usual.
+                // stays below it.) A half without a list entry counts as −∞. The first tile itself is
+                // admitted at ≥ τ₀ (one below in the strict test), later tiles at > τ as usual.
                 if (cap <= 32 && ntiles >= 2) {
                     // both accumulators hold a tile by now (tiles 0 and 1): 64 groups of 512 columns
                     if (!mbar_wait(&bars->t_full[1], 0, timeout_flag, false)) break;
                     tc_fence_after();
                     // (no stop can fall on tile 1: the warps' floors are still −inf when it is issued)
+                    int d0, d1;
+                    const bool two1 = tile_cols(1, d0, d1);
                     float gmax[64];
 #pragma unroll
                     for (int h = 0; h < 8; ++h) {
                         tmem_ld64(lane_addr + (uint32_t)((h >> 2) * BLOCK_N + 64 * (h & 3)), ra);
                         tmem_wait(ra);
                         group_max8(ra, gmax + 8 * h);
+                        if ((h & 3) >= 2 && !((h >> 2) ? two1 : two))
+#pragma unroll
+                            for (int g = 0; g < 8; ++g) gmax[8 * h + g] = -CUDART_INF_F;
                     }
                     tau = nextafterf(kth_of<64>(gmax, cap), -CUDART_INF_F);
                 } else if (cap <= 32) {
@@ -658,6 +700,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         tmem_ld64(tb + (uint32_t)(64 * h), ra);
                         tmem_wait(ra);
                         group_max8(ra, gmax + 8 * h);
+                        if (h >= 2 && !two)
+#pragma unroll
+                            for (int g = 0; g < 8; ++g) gmax[8 * h + g] = -CUDART_INF_F;
                     }
                     tau = nextafterf(kth_of<32>(gmax, cap), -CUDART_INF_F);
                 } else {
@@ -667,39 +712,46 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         tmem_ld64(tb + (uint32_t)(64 * h), ra);
                         tmem_wait(ra);
                         group_max4(ra, gmax + 16 * h);
+                        if (h >= 2 && !two)
+#pragma unroll
+                            for (int g = 0; g < 16; ++g) gmax[16 * h + g] = -CUDART_INF_F;
                     }
                     tau = nextafterf(kth_of<64>(gmax, cap), -CUDART_INF_F);
                 }
             }
-            // Four 64-column slices, as a two-step software pipeline: the next slice's TMEM load is
-            // in flight while one is scanned. A slice costs a max tree and a warp OR; only the
-            // 8-column groups some lane needs are re-read and scanned.
+            // Four 64-column slices (two per half), as a two-step software pipeline: the next
+            // slice's TMEM load is in flight while one is scanned. A slice costs a max tree and a warp
+            // OR; only the 8-column groups some lane needs are re-read and scanned.
             tmem_ld64(tb, ra);
             tmem_wait(ra);
 #pragma unroll 1
             for (int h = 0; h < 2; ++h) {
-                tmem_ld64(tb + (uint32_t)(128 * h + 64), rb);
+                const int ch = h ? c1 : c0;  // the half's first column
+                tmem_ld64(tb + (uint32_t)(HALF_N * h + 64), rb);
                 unsigned gm = slice_mask(ra, tau);
                 if (gm) {
                     cnt_m = cnt;
                     tau_m = tau;
-                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h), c0 + 128 * h, n, q, qi, qbase, lane, cap, q_lo, B_s,
-                                     B_i, &cnt_m, &tau_m);
+                    admit_groups<SL>(gm, tb + (uint32_t)(HALF_N * h), ch, n, q, qi, qbase, lane, cap, q_lo, B_s, B_i,
+                                     &cnt_m, &tau_m);
                     cnt = cnt_m;
                     tau = tau_m;
                 }
                 tmem_wait(rb);
-                if (h == 0) tmem_ld64(tb + 128, ra);
+                if (h == 0 && two) tmem_ld64(tb + HALF_N, ra);
                 gm = slice_mask(rb, tau);
                 if (gm) {
                     cnt_m = cnt;
                     tau_m = tau;
-                    admit_groups<SL>(gm, tb + (uint32_t)(128 * h + 64), c0 + 128 * h + 64, n, q, qi, qbase, lane, cap,
-                                     q_lo, B_s, B_i, &cnt_m, &tau_m);
+                    admit_groups<SL>(gm, tb + (uint32_t)(HALF_N * h + 64), ch + 64, n, q, qi, qbase, lane, cap, q_lo,
+                                     B_s, B_i, &cnt_m, &tau_m);
                     cnt = cnt_m;
                     tau = tau_m;
                 }
-                if (h == 0) tmem_wait(ra);
+                if (h == 0) {
+                    if (!two) break;
+                    tmem_wait(ra);
+                }
             }
             // every TMEM read of this accumulator is complete: hand it back to the MMA warp
             tc_fence_before();
@@ -1299,13 +1351,15 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
 }
 
 cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const float* list_ub,
-                          const uint32_t* counts, int ncb, uint32_t* cand_idx, float* cand_score, float* tau,
-                          unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
-                          cudaStream_t st, int qb0, int qb1) {
+                          const uint32_t* counts, int ncb, int list_cb, uint32_t* cand_idx, float* cand_score,
+                          float* tau, unsigned long long* stopped_total, unsigned long long* timeout_flag,
+                          int sm_count, cudaStream_t st, int qb0, int qb1) {
     (void)sm_count;
+    if (lists && list_cb != HALF_N && list_cb != BLOCK_N) return cudaErrorInvalidValue;
+    const int epc = lists && list_cb == HALF_N ? 2 : 1;  // list entries per tile
     CUtensorMap ma, mb;
     if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M, plan.fp8) ||
-        !make_map(&mb, plan.ops_b, plan.kpb, plan.np, BLOCK_N, plan.fp8))
+        !make_map(&mb, plan.ops_b, plan.kpb, plan.np, HALF_N, plan.fp8))
         return cudaErrorInvalidValue;
     const Shape sh = plan.fp8 ? shape_fp8(plan.d) : shape_of(plan.d);
     const size_t fixed = fixed_smem(sh, cap), per = stage_smem(sh);
@@ -1323,8 +1377,9 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,
-                                            cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, plan.row_eps,
-                                            cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0); note_launch();
+                                            cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, epc,
+                                            plan.row_eps, cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0);
+    note_launch();
     return cudaGetLastError();
 }
 

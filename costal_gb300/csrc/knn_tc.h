@@ -32,14 +32,15 @@ size_t workspace_bytes(int n, int d, bool fp8 = false);
 cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, const uint32_t* perm, cudaStream_t st,
                     Plan& plan, bool fp8 = false);
 // All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
-// With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]);
-// with list_ub (their bounds, non-increasing) it stops once no later block can hold an admissible
-// column for any of its rows. [qb0, qb1) restricts the launch to those query blocks (one shard of
-// the rows); qb1 = -1 means all of them.
+// With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]) of
+// list_cb working rows each (128: two list entries fill one 256-column tile; 256: one); with list_ub
+// (their bounds, non-increasing) it stops once no later block can hold an admissible column for any
+// of its rows. [qb0, qb1) restricts the launch to those query blocks (one shard of the rows); qb1 = -1
+// means all of them.
 cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, const float* list_ub,
-                          const uint32_t* counts, int ncb, uint32_t* cand_idx, float* cand_score, float* tau,
-                          unsigned long long* stopped_total, unsigned long long* timeout_flag, int sm_count,
-                          cudaStream_t st, int qb0 = 0, int qb1 = -1);
+                          const uint32_t* counts, int ncb, int list_cb, uint32_t* cand_idx, float* cand_score,
+                          float* tau, unsigned long long* stopped_total, unsigned long long* timeout_flag,
+                          int sm_count, cudaStream_t st, int qb0 = 0, int qb1 = -1);
 
 // Per-row block bounds for the column lists (prune.cu): for every query block Q (128 working rows)
 // and column block B with unit centre c_B (centers_fT: [d][ncb] f32), rowmax[Q·ncb + B] = the largest

@@ -8,7 +8,8 @@
 //             deterministic centroid sums) and the cell of every row;
 //   order     a working order: rows stably sorted by cell (ties by original index). The tensor
 //             operands are laid out in this order; candidates are mapped back to original indices.
-//   geometry  for every 128-row query block Q and every 256-row column block B (in working order) a
+//   geometry  for every 128-row query block Q and every column block B (128 working rows, or 256 for
+//             lists longer than the sort takes; prune.h col_block) a
 //             unit centre c and an angular radius r = max angle(row, c), in f64;
 //   bound     for q ∈ Q, x ∈ B: angle(q, x) ≥ angle(c_Q, c_B) − r_Q − r_B (the angle is a metric on
 //             the sphere), so cos(q, x) ≤ UB(Q, B) = cos(max(0, angle(c_Q, c_B) − r_Q − r_B − ξ)),
@@ -570,7 +571,8 @@ inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 bool supported(int d) { return d >= 1 && d <= 64; }
 
 size_t workspace_bytes(int n, int d) {
-    const size_t nqb = (size_t)(n + QB - 1) / QB, ncb = (size_t)(n + CB - 1) / CB;
+    const int cb = col_block(n);
+    const size_t nqb = (size_t)(n + QB - 1) / QB, ncb = (size_t)(n + cb - 1) / cb;
     const size_t m = (size_t)(n < SAMPLE ? n : SAMPLE), nch = (size_t)(n + CHUNK - 1) / CHUNK;
     return a256(n * 4ull) * 2 + a256((size_t)K_CENTROIDS * d * 4) + a256(nqb * d * 8) + a256(nqb * 8) +
            a256(ncb * d * 8) + a256(ncb * 8) + a256(ncb * d * 4) + a256(ncb * 4) + 2 * a256(nqb * ncb * 4) +
@@ -605,7 +607,8 @@ __global__ void k_init_centroids(const float* rows, int m, int d, int K, float* 
 
 cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaStream_t st, Plan& P) {
     const int K = K_CENTROIDS;
-    const int nqb = (n + QB - 1) / QB, ncb = (n + CB - 1) / CB;
+    const int cb = col_block(n);
+    const int nqb = (n + QB - 1) / QB, ncb = (n + cb - 1) / cb;
     const int m = n < SAMPLE ? n : SAMPLE, nch = (n + CHUNK - 1) / CHUNK;
     char* p = static_cast<char*>(ws);
     auto take = [&](size_t bytes) {
@@ -618,6 +621,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     P.K = K;
     P.nqb = nqb;
     P.ncb = ncb;
+    P.cb = cb;
     P.perm = reinterpret_cast<uint32_t*>(take(n * 4ull));
     P.cell = reinterpret_cast<uint32_t*>(take(n * 4ull));
     P.centroids = reinterpret_cast<float*>(take((size_t)K * d * 4));
@@ -660,7 +664,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     // the rows in working order, row-major, for the block geometry's contiguous reads
     k_gather_rows<<<std::min((n * d + 255) / 256, 8 * 1024), 256, 0, st>>>(xsT, np, d, P.perm, n, S.wrows); note_launch();
     k_block_geom<<<nqb, 256, 0, st>>>(S.wrows, d, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
-    k_block_geom<<<ncb, 256, 0, st>>>(S.wrows, d, n, CB, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f); note_launch();
+    k_block_geom<<<ncb, 256, 0, st>>>(S.wrows, d, n, cb, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f); note_launch();
     return cudaGetLastError();
 }
 
@@ -729,8 +733,8 @@ cudaError_t norm_order(const double* norms, int n, void* ws, uint32_t* perm, cud
 }
 
 cudaError_t build_lists(Plan& P, unsigned long long* skipped_total, cudaStream_t st) {
-    // up to 8,192 column blocks (n ≤ 2,097,152): 16 keys a thread, two CTAs per SM; up to 16,384
-    // (n ≤ 4,194,304): 32 keys a thread; beyond that the lists stay in block order (no early stop)
+    // up to 8,192 column blocks: 16 keys a thread, two CTAs per SM; up to 16,384: 32 keys a thread;
+    // beyond that (n > 4,194,304 with blocks of 256) the lists stay in block order (no early stop)
     const bool wide = P.ncb > ListShape<16>::N;
     auto kern = wide ? k_block_lists<32> : k_block_lists<16>;
     const size_t smem = (size_t)(wide ? ListShape<32>::N : ListShape<16>::N) * 4;

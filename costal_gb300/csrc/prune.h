@@ -10,12 +10,22 @@ namespace prune {
 
 constexpr int K_CENTROIDS = 256;  // spherical k-means cells
 constexpr int QB = 128;           // query block (rows of one tensor-core CTA)
-constexpr int CB = 256;           // column block (one tensor-core tile)
+// Column blocks: 128 working rows (half a tensor-core tile; the coarse kernel fills a tile from two
+// list entries) while a query block's list fits the 16-keys-a-thread sort (≤ 8,192 blocks, n ≤
+// 1,048,576), else 256 (one tile per entry). Blocks of 128 straddle fewer k-means cells, so their
+// bounds skip more columns (visited pairs 25 % instead of 36 % at 200,000 rows of the Zipf mixture, 14.1
+// instead of 15.1 % at 2,000,000), but twice as many list entries cost more to bound and sort: measured
+// per step they win up to 1,000,000 rows (−6.6 % at 200,000, −1.9 % at 1,000,000) and lose at
+// 2,000,000 (+5.5 %), where the lists need the 32-keys-a-thread sort.
+constexpr int CB_FINE = 128, CB_WIDE = 256;
+constexpr int LIST_FAST = 8192;  // the widest list of the 16-keys-a-thread sort
+inline int col_block(int n) { return (n + CB_FINE - 1) / CB_FINE <= LIST_FAST ? CB_FINE : CB_WIDE; }
 constexpr int SAMPLE = 65536;     // rows of the k-means sample
 constexpr int LLOYD_STEPS = 8;
 
 struct Plan {
     int n, d, K, nqb, ncb;
+    int cb;              // rows of a column block (col_block(n))
     uint32_t* perm;      // working -> original [n]
     uint32_t* cell;      // cell of every original row [n]
     float* centroids;    // [K][d] unit centroids

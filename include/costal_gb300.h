@@ -207,9 +207,9 @@ int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, cons
                         float quantile, float* grad, char* err, size_t errlen);
 /* Test hook: the per-row block bound data of the tensor-core path for X (host, n x d, 1 <= d <= 64):
  * the working order perm[n] (working -> original row), the column blocks' unit centres ccenter[ncb][d]
- * and angular radii cradius[ncb] (f64, blocks of 256 working rows), rowmax[nqb][ncb] = the largest
- * split-BF16 coarse score of a query block's rows (blocks of 128) with each centre, and *delta, its
- * error margin in cosine; nqb = ceil(n/128), ncb = ceil(n/256). */
+ * and angular radii cradius[ncb] (f64, blocks of cb working rows: 128 while ceil(n/128) <= 8192, else
+ * 256), rowmax[nqb][ncb] = the largest split-BF16 coarse score of a query block's rows (blocks of 128)
+ * with each centre, and *delta, its error margin in cosine; nqb = ceil(n/128), ncb = ceil(n/cb). */
 int costal_block_bounds(const float* x, uint64_t n, uint32_t d, uint32_t* perm, double* ccenter, double* cradius,
                         float* rowmax, float* delta, char* err, size_t errlen);
 
