@@ -400,12 +400,13 @@ __device__ __noinline__ void admit_groups(unsigned gmask, uint32_t taddr, int cb
     *tau_io = tau;
 }
 
-template <int SLOTS, bool KLOOP, bool FP8 = false>
+template <int SLOTS, bool KLOOP, bool FP8 = false, bool PAIR = false>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int n, int np,
+    k_coarse_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                const __grid_constant__ CUtensorMap map_bw, int n, int np,
                 int nkb, int nkb_b, int ksteps, int k1s, int stages, int cap, const uint32_t* __restrict__ perm,
                 const uint32_t* __restrict__ lists, const float* __restrict__ list_ub,
-                const uint32_t* __restrict__ counts, int ncb, int epc, const double* __restrict__ row_eps,
+                const uint32_t* __restrict__ counts, int ncb, const double* __restrict__ row_eps,
                 uint32_t* __restrict__ cand_idx, float* __restrict__ cand_score, float* __restrict__ tau_out,
                 unsigned long long* __restrict__ stopped_total, unsigned long long* __restrict__ timeout_flag,
                 int qb0) {
@@ -435,35 +436,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // CTA b takes query block qb0 + b (a launch over a contiguous range of query blocks: one shard).
     const int qb = qb0 + (int)blockIdx.x;
     const int q0 = qb * BLOCK_M;
-    // A tile's 256 columns are two halves of HALF_N, each loaded by its own TMA box: with lists of
-    // 128-column blocks (epc = 2) two consecutive list entries, with lists of 256-column blocks (epc =
-    // 1) one entry, without lists 256 consecutive columns. An odd list's last tile has one entry; its
-    // second half repeats the first and the epilogue leaves it out.
+    // A tile's 256 columns are two halves of HALF_N. PAIR (lists of 128-column blocks): the halves are
+    // two consecutive list entries, each loaded by its own TMA box unless they are adjacent; an odd
+    // list's last tile has one entry, its second half repeats the first and the epilogue leaves it out.
+    // Otherwise one list entry of 256 columns, or without lists 256 consecutive columns. (The pairing
+    // is a compile-time choice: the epilogue is latency-bound, and its runtime tests cost 3 % of the
+    // kernel when the lists hold 256-column blocks.)
+    constexpr int EPC = PAIR ? 2 : 1;  // list entries per tile
     const int nentries = lists ? (int)counts[qb] : 0;
-    const int ntiles = lists ? (nentries + epc - 1) / epc : np / BLOCK_N;
+    const int ntiles = lists ? (nentries + EPC - 1) / EPC : np / BLOCK_N;
     const uint32_t* my_list = lists ? lists + (size_t)qb * ncb : nullptr;
     auto tile_cols = [&](int t, int& c0, int& c1) -> bool {
-        if (!my_list) {
-            c0 = t * BLOCK_N;
+        if constexpr (PAIR) {
+            const bool two = 2 * t + 1 < nentries;
+            c0 = (int)my_list[2 * t] * HALF_N;
+            c1 = two ? (int)my_list[2 * t + 1] * HALF_N : c0;
+            return two;
+        } else {
+            c0 = (my_list ? (int)my_list[t] : t) * BLOCK_N;
             c1 = c0 + HALF_N;
             return true;
         }
-        if (epc == 1) {
-            c0 = (int)my_list[t] * BLOCK_N;
-            c1 = c0 + HALF_N;
-            return true;
-        }
-        const bool two = 2 * t + 1 < nentries;
-        c0 = (int)my_list[2 * t] * HALF_N;
-        c1 = two ? (int)my_list[2 * t + 1] * HALF_N : c0;
-        return two;
     };
     // the list entries of tile t lie inside the operands (the list kernel never writes others)
     auto tile_ok = [&](int t) -> bool {
         if (!my_list) return true;
-        const unsigned lim = (unsigned)(np / (epc == 1 ? BLOCK_N : HALF_N));
-        if (epc == 1) return my_list[t] < lim;
-        return my_list[2 * t] < lim && (2 * t + 1 >= nentries || my_list[2 * t + 1] < lim);
+        if constexpr (PAIR) {
+            const unsigned lim = (unsigned)(np / HALF_N);
+            return my_list[2 * t] < lim && (2 * t + 1 >= nentries || my_list[2 * t + 1] < lim);
+        } else {
+            return my_list[t] < (unsigned)(np / BLOCK_N);
+        }
     };
     const uint32_t a_bytes = (uint32_t)nkb * A_KB_BYTES, b_bytes = (uint32_t)nkb_b * B_KB_BYTES;
     (void)a_bytes;
@@ -517,10 +520,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         } else if (t > 0 && my_ub) {
                             volatile float* wf = bars->warp_floor;
                             const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
-                            if (my_ub[t * epc] < fl) {
+                            if (my_ub[t * EPC] < fl) {
                                 stop = true;
                                 if (stopped_total)
-                                    atomicAdd(stopped_total, (unsigned long long)(nentries - t * epc));
+                                    atomicAdd(stopped_total, (unsigned long long)(nentries - t * EPC));
                             }
                         }
                         if (stop) {
@@ -533,8 +536,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     mbar_expect_tx(&bars->b_full[s], (uint32_t)(A_KB_BYTES + B_KB_BYTES));
                     unsigned char* dst = b_tiles + (size_t)s * stage_bytes;
                     tma_load_2d(dst, &map_a, kb * KBE, q0, &bars->b_full[s]);
-                    tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
-                    tma_load_2d(dst + A_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
+                    if (c1 == c0 + HALF_N) {  // adjacent halves: one 256-row box
+                        tma_load_2d(dst + A_KB_BYTES, &map_bw, kb * KBE, c0, &bars->b_full[s]);
+                    } else {
+                        tma_load_2d(dst + A_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
+                        tma_load_2d(dst + A_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
+                    }
                 }
             }
         }
@@ -561,9 +568,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     // floors read may be stale, i.e. lower, which only delays the stop.
                     volatile float* wf = bars->warp_floor;
                     const float fl = fminf(fminf(wf[0], wf[1]), fminf(wf[2], wf[3]));
-                    if (my_ub[t * epc] < fl) {
+                    if (my_ub[t * EPC] < fl) {
                         *reinterpret_cast<volatile int*>(&bars->stop_tile) = t;
-                        if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(nentries - t * epc));
+                        if (stopped_total) atomicAdd(stopped_total, (unsigned long long)(nentries - t * EPC));
                         mbar_arrive(&bars->b_full[s]);  // completes the phase without data (release)
                         break;
                     }
@@ -574,9 +581,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 tile_cols(t, c0, c1);
                 // (the last K block may reach past the operand's row: TMA fills those columns with zeros
                 // and reads nothing for them)
-                for (int kb = 0; kb < nkb_b; ++kb) {
-                    tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
-                    tma_load_2d(dst + kb * B_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
+                if (c1 == c0 + HALF_N) {  // adjacent halves: one 256-row box per K block
+                    for (int kb = 0; kb < nkb_b; ++kb)
+                        tma_load_2d(dst + kb * B_KB_BYTES, &map_bw, kb * KBE, c0, &bars->b_full[s]);
+                } else {
+                    for (int kb = 0; kb < nkb_b; ++kb) {
+                        tma_load_2d(dst + kb * B_KB_BYTES, &map_b, kb * KBE, c0, &bars->b_full[s]);
+                        tma_load_2d(dst + kb * B_KB_BYTES + B_HALF_BYTES, &map_b, kb * KBE, c1, &bars->b_full[s]);
+                    }
                 }
             }
         }
@@ -1357,9 +1369,10 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     (void)sm_count;
     if (lists && list_cb != HALF_N && list_cb != BLOCK_N) return cudaErrorInvalidValue;
     const int epc = lists && list_cb == HALF_N ? 2 : 1;  // list entries per tile
-    CUtensorMap ma, mb;
+    CUtensorMap ma, mb, mbw;  // the column operand in boxes of one half tile and of a whole tile
     if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M, plan.fp8) ||
-        !make_map(&mb, plan.ops_b, plan.kpb, plan.np, HALF_N, plan.fp8))
+        !make_map(&mb, plan.ops_b, plan.kpb, plan.np, HALF_N, plan.fp8) ||
+        !make_map(&mbw, plan.ops_b, plan.kpb, plan.np, BLOCK_N, plan.fp8))
         return cudaErrorInvalidValue;
     const Shape sh = plan.fp8 ? shape_fp8(plan.d) : shape_of(plan.d);
     const size_t fixed = fixed_smem(sh, cap), per = stage_smem(sh);
@@ -1370,15 +1383,18 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
     if (qb1 < 0) qb1 = qblocks;
     if (qb0 < 0 || qb1 > qblocks || qb0 >= qb1) return cudaErrorInvalidValue;
+    const bool pair = epc == 2;
     auto kern = plan.fp8 ? (cap <= 32 ? k_coarse_tc<1, true, true> : k_coarse_tc<2, true, true>)
-                : !sh.resident ? (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>)
-                               : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>);
+                : !sh.resident ? (pair ? (cap <= 32 ? k_coarse_tc<1, true, false, true> : k_coarse_tc<2, true, false, true>)
+                                       : (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>))
+                               : (pair ? (cap <= 32 ? k_coarse_tc<1, false, false, true> : k_coarse_tc<2, false, false, true>)
+                                       : (cap <= 32 ? k_coarse_tc<1, false> : k_coarse_tc<2, false>));
+    if (plan.fp8 && pair) return cudaErrorInvalidValue;  // (deep rows never get lists)
     if (plan.fp8 && sh.resident) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,
-                                            cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, epc,
-                                            plan.row_eps, cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0);
+    kern<<<qb1 - qb0, NTHREADS, smem, st>>>(ma, mb, mbw, plan.n, plan.np, sh.nkb_a, sh.nkb_b, sh.ksteps, sh.k1s, stages,
+                                            cap, plan.perm, lists, lists ? list_ub : nullptr, counts, ncb, plan.row_eps, cand_idx, cand_score, tau, stopped_total, timeout_flag, qb0);
     note_launch();
     return cudaGetLastError();
 }
