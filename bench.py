@@ -300,6 +300,9 @@ def main():
     ap.add_argument("--train-sample", type=int, default=200_000)
     ap.add_argument("--train-epochs", type=int, default=60)
     ap.add_argument("--train-quantile", type=float, default=0.01, help="pinball-loss quantile of the model")
+    ap.add_argument("--mlp-save", default=None, help="write the trained model here (.npz)")
+    ap.add_argument("--mlp-load", default=None,
+                    help="load a model saved with --mlp-save instead of training (e.g. to profile the steps alone)")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed steps of the plain FP32 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -361,7 +364,13 @@ def main():
 
     # ---- the model (trained once on this input, labels from the plain FP32 path; untimed)
     train = None
-    if learned:
+    if learned and args.mlp_load:
+        from costal_gb300 import _costal as ext
+
+        z = np.load(args.mlp_load)
+        ext._mlp_set(z["params"], int(z["d"]), int(z["k"]), float(z["quantile"]))
+        train = {"loaded": args.mlp_load}
+    elif learned:
         mo = L.MlpOpts()
         mo.sample, mo.epochs, mo.batch = min(args.train_sample, n), args.train_epochs, 2048
         mo.margin, mo.lr, mo.quantile, mo.seed = wl.margin, 2e-3, args.train_quantile, 20241203
@@ -371,6 +380,11 @@ def main():
                 err)
         train = {kk: v for kk, v in ms_.as_dict().items()}
         train["wall_s"] = time.perf_counter() - t
+        if args.mlp_save:
+            from costal_gb300 import _costal as ext
+
+            params, md, mk, mq = ext._mlp_get()
+            np.savez(args.mlp_save, params=params, d=md, k=mk, quantile=mq)
 
     dx = torch.from_numpy(x).cuda()
     d_rows = torch.empty(n * k, dtype=torch.int32, device="cuda")
@@ -594,7 +608,7 @@ def main():
                                              "ms_total")},
             "clocks": clocks.summary(),
         }
-        if train is not None:
+        if train is not None and "ms_train" in train:
             line["value_incl_training"] = job_cells_per_s(n, 1, ms + train["ms_labels"] + train["ms_train"])
         if not args.no_cpu:
             v, cores, sample = cpu_baseline(x, wl, target_s=args.cpu_seconds)
