@@ -336,7 +336,8 @@ void run_knn(Context& c, const float* d_x, int n, int d, int k, const costal_knn
             CK(ensure(c.tc_ws, tc::workspace_bytes(n, d, fp8)));
             CK(ensure(c.tc_rows, (size_t)n * 4));
             tc::Plan plan{};
-            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan, fp8));
+            CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), n, np, dp, d, ordered ? pp.perm : nullptr, s, plan, fp8,
+                           ordered && !fp8 ? pp.wrows : nullptr));
             if (ordered) {
                 // with the early stop, the lists take the per-row bound too (the nearest row of each
                 // query block to each column block's centre, from the split operands just made)
@@ -1085,7 +1086,7 @@ int costal_block_bounds(const float* x, uint64_t n, uint32_t d, uint32_t* perm, 
         CK(prune::build_order(c.prune_ws.p, c.xsT.as<float>(), N, np, D, s, pp));
         CK(ensure(c.tc_ws, tc::workspace_bytes(N, D, false)));
         tc::Plan plan{};
-        CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), N, np, dp, D, pp.perm, s, plan, false));
+        CK(tc::prepare(c.tc_ws.p, c.xsT.as<float>(), N, np, dp, D, pp.perm, s, plan, false, pp.wrows));
         CK(ensure(c.rm_ws, tc::rowmax_bytes(pp.ncb, D)));
         CK(ensure(c.rm_out, (size_t)pp.nqb * pp.ncb * 4));
         const float* d_delta = nullptr;

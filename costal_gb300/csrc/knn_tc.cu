@@ -958,17 +958,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
 // ---- operand preparation ----------------------------------------------------------------------
 
-// One CTA per 128 working rows: each thread splits its row (read from xsT at the original index)
-// into the two operands in shared memory and records the f64 norms of the pieces: [0] ‖a_hi‖,
+// One CTA per 128 working rows: each thread splits its row (read from xsT at the original index, or
+// from wrows, the rows already in working order, row-major: a row's values are then contiguous instead
+// of one cache line each) into the two operands in shared memory and records the f64 norms of the pieces: [0] ‖a_hi‖,
 // [1] ‖a_lo‖, [2] ‖r‖, [3] ‖a_hi + a_lo‖; then the CTA writes the 128 operand rows with coalesced
 // word stores. Rows in [n, rows) are written as zeros. The maxima over rows go to colmax through one
 // atomic per warp. Two layouts: compact (k1 > 0) A = [hi | hi | 0 … k1 | lo | 0 … kpa] and
 // B = [hi | lo | 0 … kpb]; otherwise A = [hi | lo | hi | 0 … kp], B = [hi | hi | lo | 0 … kp].
 constexpr int SPLIT_ROWS = 128;
 __global__ void __launch_bounds__(SPLIT_ROWS)
-    k_split(const float* __restrict__ xsT, int n, int np_x, int rows, int d, int kpa, int kpb, int k1,
-            const uint32_t* __restrict__ perm, __nv_bfloat16* __restrict__ opa, __nv_bfloat16* __restrict__ opb,
-            double* __restrict__ pnorm, unsigned long long* __restrict__ colmax) {
+    k_split(const float* __restrict__ xsT, const float* __restrict__ wrows, int n, int np_x, int rows, int d, int kpa,
+            int kpb, int k1, const uint32_t* __restrict__ perm, __nv_bfloat16* __restrict__ opa,
+            __nv_bfloat16* __restrict__ opb, double* __restrict__ pnorm, unsigned long long* __restrict__ colmax) {
     extern __shared__ uint32_t sw[];  // [SPLIT_ROWS][kpa/2 + 1] then [SPLIT_ROWS][kpb/2 + 1] words
     const int wsa = kpa / 2 + 1, wsb = kpb / 2 + 1;  // odd word strides: the 32 lanes' rows fall in 32 banks
     __nv_bfloat16* ta = reinterpret_cast<__nv_bfloat16*>(sw);
@@ -983,7 +984,7 @@ __global__ void __launch_bounds__(SPLIT_ROWS)
     for (int t = 0; t < kpa; ++t) ra[t] = zero;
     for (int t = 0; t < kpb; ++t) rb[t] = zero;
     for (int t = 0; t < d; ++t) {
-        const float a = live ? xsT[(size_t)t * np_x + o] : 0.0f;
+        const float a = live ? (wrows ? wrows[(size_t)r * d + t] : xsT[(size_t)t * np_x + o]) : 0.0f;
         const __nv_bfloat16 hb = __float2bfloat16_rn(a);
         const float h = __bfloat162float(hb);
         const float e = a - h;  // exact in f32
@@ -1323,7 +1324,7 @@ Layout carve(void* ws, int n, int d, bool fp8) {
 }  // namespace
 
 cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, const uint32_t* perm, cudaStream_t st,
-                    Plan& plan, bool fp8) {
+                    Plan& plan, bool fp8, const float* wrows) {
     (void)dp;
     const int np = (n + 255) / 256 * 256;  // the tensor tiles are 256 columns wide
     const Shape sh = fp8 ? shape_fp8(d) : shape_of(d);
@@ -1338,7 +1339,7 @@ cudaError_t prepare(void* ws, const float* xsT, int n, int np_x, int dp, int d, 
     } else if (smem <= 227 * 1024) {
         e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, n, np_x, np, d, sh.kpa, sh.kpb,
+        k_split<<<np / SPLIT_ROWS, SPLIT_ROWS, smem, st>>>(xsT, wrows, n, np_x, np, d, sh.kpa, sh.kpb,
                                                             sh.compact ? sh.k1s * 16 : 0, perm,
                                                             static_cast<__nv_bfloat16*>(L.opa),
                                                             static_cast<__nv_bfloat16*>(L.opb), L.pnorm, L.colmax);
@@ -1467,7 +1468,7 @@ cudaError_t launch_rowmax(const Plan& plan, const float* centers_fT, int ncb, vo
     const size_t ssm = (size_t)SPLIT_ROWS * (sh.kpa / 2 + 1 + sh.kpb / 2 + 1) * 4;
     if ((e = cudaFuncSetAttribute(k_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm)) != cudaSuccess)
         return e;
-    k_split<<<rows / SPLIT_ROWS, SPLIT_ROWS, ssm, st>>>(centers_fT, ncb, ncb, rows, plan.d, sh.kpa, sh.kpb,
+    k_split<<<rows / SPLIT_ROWS, SPLIT_ROWS, ssm, st>>>(centers_fT, nullptr, ncb, ncb, rows, plan.d, sh.kpa, sh.kpb,
                                                          sh.compact ? sh.k1s * 16 : 0, nullptr,
                                                          static_cast<__nv_bfloat16*>(L.opa),
                                                          static_cast<__nv_bfloat16*>(L.opb), L.pnorm, L.colmax);

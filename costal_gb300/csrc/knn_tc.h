@@ -28,9 +28,10 @@ bool supported(int d, int cap);
 bool supported_fp8(int d, int cap);
 size_t workspace_bytes(int n, int d, bool fp8 = false);
 // Split the normalised rows (xsT, d_pad × n_pad) into BF16 operands and per-row error norms, and
-// derive each row's certificate bound.
+// derive each row's certificate bound. wrows (optional, split BF16 only): the same rows already in the
+// working order, row-major [n][d] (prune::Plan::wrows), read instead of gathering xsT through perm.
 cudaError_t prepare(void* ws, const float* xsT, int n, int np, int dp, int d, const uint32_t* perm, cudaStream_t st,
-                    Plan& plan, bool fp8 = false);
+                    Plan& plan, bool fp8 = false, const float* wrows = nullptr);
 // All (query tile × column tile) products on tcgen05, fused with the per-query top-cap selection.
 // With lists/counts (prune.cu), CTA Q visits only the column blocks lists[Q·ncb .. + counts[Q]) of
 // list_cb working rows each (128: two list entries fill one 256-column tile; 256: one); with list_ub

@@ -39,15 +39,18 @@ __host__ __device__ inline Off offsets(int F) {
 }
 
 // ---- features ---------------------------------------------------------------------------------
-// One warp per row: the row's (at most 64) coordinates loaded once, two per lane, and broadcast by
+// One warp per row (two rows at a time, interleaved): the row's (at most 64) coordinates loaded once, two per lane, and broadcast by
 // shuffles; lane L takes the 8 consecutive centroids 8L … 8L + 7, read as two 16-byte words per
 // dimension from a transposed shared copy laid out so that a warp's words are contiguous (no bank
 // conflicts); then a branch-free warp bitonic sort of the 256 cosines (descending; only the values
 // are kept, so ties need no order) in which strides below 8 stay in a lane's registers, and the first
 // 64 (lanes 0-7) are kept. Each cosine is the same FMA chain over the dimensions in order.
 
-// Bitonic sort of a warp-distributed array, lane-major (position p = 8·lane + s), descending.
-__device__ __forceinline__ void warp_sort_desc_lane8(float (&v)[8], int lane) {
+// Bitonic sort of R warp-distributed arrays at once (independent sorts interleaved stage by stage, so
+// that each stage's shuffles and compare-exchanges of one array hide the latencies of the other's),
+// lane-major (position p = 8·lane + s), descending.
+template <int R>
+__device__ __forceinline__ void warp_sort_desc_lane8(float (&v)[R][8], int lane) {
 #pragma unroll
     for (int size = 2; size <= 256; size <<= 1) {
 #pragma unroll
@@ -58,18 +61,24 @@ __device__ __forceinline__ void warp_sort_desc_lane8(float (&v)[8], int lane) {
                     const int t = s ^ stride;
                     if (t > s) {
                         const bool desc = ((8 * lane + s) & size) == 0;
-                        const float hi = fmaxf(v[s], v[t]), lo = fminf(v[s], v[t]);
-                        v[s] = desc ? hi : lo;
-                        v[t] = desc ? lo : hi;
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const float hi = fmaxf(v[r][s], v[r][t]), lo = fminf(v[r][s], v[r][t]);
+                            v[r][s] = desc ? hi : lo;
+                            v[r][t] = desc ? lo : hi;
+                        }
                     }
                 }
             } else {
 #pragma unroll
                 for (int s = 0; s < 8; ++s) {
-                    const float o = __shfl_xor_sync(COSTAL_FULL_MASK, v[s], stride >> 3);
                     const int p = 8 * lane + s;
                     const bool keep_max = ((p & stride) == 0) == ((p & size) == 0);
-                    v[s] = keep_max ? fmaxf(v[s], o) : fminf(v[s], o);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const float o = __shfl_xor_sync(COSTAL_FULL_MASK, v[r][s], stride >> 3);
+                        v[r][s] = keep_max ? fmaxf(v[r][s], o) : fminf(v[r][s], o);
+                    }
                 }
             }
         }
@@ -94,36 +103,54 @@ __global__ void k_features(const float* __restrict__ xsT, int np, int d, const f
     const int lane = threadIdx.x & 31;
     const int F = d + MLP_TOPC;
     const int wpb = blockDim.x >> 5;
-    // grid-stride over rows, one warp per row: the centroids are loaded once per CTA
-    for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
-        const uint32_t r = rows ? rows[i] : (uint32_t)i;
-        const float x0 = lane < d ? xsT[(size_t)lane * np + r] : 0.0f;
-        const float x1 = lane + 32 < d ? xsT[(size_t)(lane + 32) * np + r] : 0.0f;
-        float dot[8];
+    // grid-stride over pairs of rows, one warp per pair (the two rows' chains interleave): the
+    // centroids are loaded once per CTA. A pair's second row past m repeats the first and is not stored.
+    constexpr int R2 = 2;
+    const int stride = gridDim.x * wpb;
+    for (int i0 = blockIdx.x * wpb + (threadIdx.x >> 5); i0 < m; i0 += R2 * stride) {
+        int ii[R2];
+        float x0[R2], x1[R2], dot[R2][8];
 #pragma unroll
-        for (int s = 0; s < 8; ++s) dot[s] = 0.0f;
+        for (int q = 0; q < R2; ++q) {
+            ii[q] = i0 + q * stride;
+            const int i = ii[q] < m ? ii[q] : i0;
+            const uint32_t r = rows ? rows[i] : (uint32_t)i;
+            x0[q] = lane < d ? xsT[(size_t)lane * np + r] : 0.0f;
+            x1[q] = lane + 32 < d ? xsT[(size_t)(lane + 32) * np + r] : 0.0f;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) dot[q][s] = 0.0f;
+        }
         for (int t = 0; t < d; ++t) {
-            const float a = __shfl_sync(COSTAL_FULL_MASK, t < 32 ? x0 : x1, t & 31);
             const float4 w0 = c_s4[t * (FEAT_C / 4) + lane], w1 = c_s4[t * (FEAT_C / 4) + 32 + lane];
-            dot[0] = fmaf(a, w0.x, dot[0]);
-            dot[1] = fmaf(a, w0.y, dot[1]);
-            dot[2] = fmaf(a, w0.z, dot[2]);
-            dot[3] = fmaf(a, w0.w, dot[3]);
-            dot[4] = fmaf(a, w1.x, dot[4]);
-            dot[5] = fmaf(a, w1.y, dot[5]);
-            dot[6] = fmaf(a, w1.z, dot[6]);
-            dot[7] = fmaf(a, w1.w, dot[7]);
+#pragma unroll
+            for (int q = 0; q < R2; ++q) {
+                const float a = __shfl_sync(COSTAL_FULL_MASK, t < 32 ? x0[q] : x1[q], t & 31);
+                dot[q][0] = fmaf(a, w0.x, dot[q][0]);
+                dot[q][1] = fmaf(a, w0.y, dot[q][1]);
+                dot[q][2] = fmaf(a, w0.z, dot[q][2]);
+                dot[q][3] = fmaf(a, w0.w, dot[q][3]);
+                dot[q][4] = fmaf(a, w1.x, dot[q][4]);
+                dot[q][5] = fmaf(a, w1.y, dot[q][5]);
+                dot[q][6] = fmaf(a, w1.z, dot[q][6]);
+                dot[q][7] = fmaf(a, w1.w, dot[q][7]);
+            }
         }
 #pragma unroll
-        for (int s = 0; s < 8; ++s)
-            if (8 * lane + s >= K) dot[s] = -CUDART_INF_F;
-        warp_sort_desc_lane8(dot, lane);
-        float* f = feat + (size_t)i * F;
-        if (lane < d) f[lane] = x0;
-        if (lane + 32 < d) f[lane + 32] = x1;
-        if (lane < MLP_TOPC / 8) {
+        for (int q = 0; q < R2; ++q)
 #pragma unroll
-            for (int s = 0; s < 8; ++s) f[d + 8 * lane + s] = dot[s];
+            for (int s = 0; s < 8; ++s)
+                if (8 * lane + s >= K) dot[q][s] = -CUDART_INF_F;
+        warp_sort_desc_lane8<R2>(dot, lane);
+#pragma unroll
+        for (int q = 0; q < R2; ++q) {
+            if (ii[q] >= m) continue;
+            float* f = feat + (size_t)ii[q] * F;
+            if (lane < d) f[lane] = x0[q];
+            if (lane + 32 < d) f[lane + 32] = x1[q];
+            if (lane < MLP_TOPC / 8) {
+#pragma unroll
+                for (int s = 0; s < 8; ++s) f[d + 8 * lane + s] = dot[q][s];
+            }
         }
     }
 }
@@ -169,11 +196,14 @@ __device__ void forward_block(const float* __restrict__ P, int F, const float* _
 
 // ---- inference ----------------------------------------------------------------------------------
 // Persistent CTAs of 256 threads: the weights, transposed, stay in shared memory while the CTA walks
-// 64-row tiles. Thread (ty, tx) = (tid / 16, tid % 16) holds a 4-row × 8-unit register tile: per
-// input feature one float4 of the (transposed) activations and two float4 of weights feed 32 FMAs.
-// Every hidden unit's sum runs bias first, then the inputs in order, like forward_block; the output
-// adds 16 partial sums of 8 units in a fixed tree.
-constexpr int IR = 64;        // rows per tile
+// 128-row tiles. Thread (ty, tx) = (tid / 16, tid % 16) holds an 8-row × 8-unit register tile: rows
+// 4ty … 4ty+3 and 64+4ty … 64+4ty+3, units 4tx … 4tx+3 and 64+4tx … 64+4tx+3, so that per input feature
+// two float4 of activations (the same for the 16 threads of a half-warp) and two float4 of weights (16
+// consecutive float4 across the half-warp: no bank conflicts) feed 64 FMAs. One buffer holds the tile's
+// features, transposed, and then its layer-1 activations. Every hidden unit's sum runs bias first,
+// then the inputs in order, like forward_block; the output adds the 16 threads' partial sums of 8 units
+// in a fixed tree.
+constexpr int IR = 128;       // rows per tile
 constexpr int IT = 256;       // threads
 constexpr int IRS = IR + 4;   // row stride of the transposed activations (float4-aligned)
 
@@ -185,8 +215,7 @@ __global__ void __launch_bounds__(IT, 1) k_infer(const float* __restrict__ P, in
     float* b1 = w2t + MLP_H * MLP_H;            // [H]
     float* b2 = b1 + MLP_H;                     // [H]
     float* w3 = b2 + MLP_H;                     // [H]
-    float* ft = w3 + MLP_H;                     // [F][IRS] features, transposed
-    float* h1t = ft + (size_t)F * IRS;          // [H][IRS] layer-1 activations, transposed
+    float* act = w3 + MLP_H;                    // [max(F, H)][IRS]: features, then layer-1 activations
     const Off o = offsets(F);
     const int tid = threadIdx.x;
     for (int e = tid; e < MLP_H * F; e += IT) {
@@ -204,73 +233,72 @@ __global__ void __launch_bounds__(IT, 1) k_infer(const float* __restrict__ P, in
     }
     const float b3 = P[o.b3];
     const int ty = tid >> 4, tx = tid & 15;
+    const int ra = 4 * ty, rb = 64 + 4 * ty;  // the thread's two groups of 4 rows
+    const int ua = 4 * tx, ub = 64 + 4 * tx;  // and of 4 units
     const int ntiles = (m + IR - 1) / IR;
+    float acc[8][8];
+    // one layer: acc[i][j] = bias(unit j) + Σ_t w(t, unit j)·x(t, row i), t in order
+    auto layer = [&](const float* wt, const float* bias, int K) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float b = bias[j < 4 ? ua + j : ub + j - 4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i][j] = b;
+        }
+        for (int t = 0; t < K; ++t) {
+            const float4 a0 = *reinterpret_cast<const float4*>(act + t * IRS + ra);
+            const float4 a1 = *reinterpret_cast<const float4*>(act + t * IRS + rb);
+            const float4 w0 = *reinterpret_cast<const float4*>(wt + t * MLP_H + ua);
+            const float4 w1 = *reinterpret_cast<const float4*>(wt + t * MLP_H + ub);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
+        }
+    };
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r0 = tile * IR;
-        __syncthreads();  // the previous tile's readers of ft / h1t are done (and the weights loaded)
+        __syncthreads();  // the previous tile's readers of act are done (and the weights loaded)
+        // the tile's features, read row by row (coalesced) and stored transposed
         for (int e = tid; e < IR * F; e += IT) {
-            const int r = e % IR, t = e / IR;
-            ft[t * IRS + r] = r0 + r < m ? feat[(size_t)(r0 + r) * F + t] : 0.0f;
+            const int r = e / F, t = e - r * F;
+            act[t * IRS + r] = r0 + r < m ? feat[(size_t)(r0 + r) * F + t] : 0.0f;
         }
         __syncthreads();
-        float acc[4][8];
+        layer(w1t, b1, F);
+        __syncthreads();  // every thread has read the features: act now takes the layer-1 activations
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const float b = b1[tx * 8 + j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) acc[i][j] = b;
+            const int u = j < 4 ? ua + j : ub + j - 4;
+            *reinterpret_cast<float4*>(act + u * IRS + ra) = make_float4(
+                fmaxf(acc[0][j], 0.0f), fmaxf(acc[1][j], 0.0f), fmaxf(acc[2][j], 0.0f), fmaxf(acc[3][j], 0.0f));
+            *reinterpret_cast<float4*>(act + u * IRS + rb) = make_float4(
+                fmaxf(acc[4][j], 0.0f), fmaxf(acc[5][j], 0.0f), fmaxf(acc[6][j], 0.0f), fmaxf(acc[7][j], 0.0f));
         }
-        for (int t = 0; t < F; ++t) {
-            const float4 a = *reinterpret_cast<const float4*>(ft + t * IRS + ty * 4);
-            const float4 wa = *reinterpret_cast<const float4*>(w1t + t * MLP_H + tx * 8);
-            const float4 wb = *reinterpret_cast<const float4*>(w1t + t * MLP_H + tx * 8 + 4);
-            const float av[4] = {a.x, a.y, a.z, a.w};
-            const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            *reinterpret_cast<float4*>(h1t + (tx * 8 + j) * IRS + ty * 4) =
-                make_float4(fmaxf(acc[0][j], 0.0f), fmaxf(acc[1][j], 0.0f), fmaxf(acc[2][j], 0.0f),
-                            fmaxf(acc[3][j], 0.0f));
         __syncthreads();
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float b = b2[tx * 8 + j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) acc[i][j] = b;
-        }
-        for (int t = 0; t < MLP_H; ++t) {
-            const float4 a = *reinterpret_cast<const float4*>(h1t + t * IRS + ty * 4);
-            const float4 wa = *reinterpret_cast<const float4*>(w2t + t * MLP_H + tx * 8);
-            const float4 wb = *reinterpret_cast<const float4*>(w2t + t * MLP_H + tx * 8 + 4);
-            const float av[4] = {a.x, a.y, a.z, a.w};
-            const float wv[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
-        }
+        layer(w2t, b2, MLP_H);
         // output layer: each thread's 8 units, then the 16 threads of a row group in a fixed tree
-        float p[4];
+        float p[8];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 8; ++i) {
             float z = 0.0f;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) z = fmaf(w3[tx * 8 + j], fmaxf(acc[i][j], 0.0f), z);
+            for (int j = 0; j < 8; ++j) z = fmaf(w3[j < 4 ? ua + j : ub + j - 4], fmaxf(acc[i][j], 0.0f), z);
             p[i] = z;
         }
 #pragma unroll
         for (int off = 1; off < 16; off <<= 1)
 #pragma unroll
-            for (int i = 0; i < 4; ++i) p[i] += __shfl_xor_sync(COSTAL_FULL_MASK, p[i], off);
-        if (tx == 0)
+            for (int i = 0; i < 8; ++i) p[i] += __shfl_xor_sync(COSTAL_FULL_MASK, p[i], off);
+        if (tx == 0) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (r0 + ty * 4 + i < m) out[r0 + ty * 4 + i] = b3 + p[i];
+            for (int i = 0; i < 8; ++i) {
+                const int r = r0 + (i < 4 ? ra + i : rb + i - 4);
+                if (r < m) out[r] = b3 + p[i];
+            }
+        }
     }
 }
 
@@ -403,7 +431,7 @@ cudaError_t features(const float* xsT, int np, int d, const float* centroids, in
 }
 
 static size_t infer_smem(int F) {
-    return ((size_t)F * MLP_H + MLP_H * MLP_H + 3 * MLP_H + (size_t)F * IRS + (size_t)MLP_H * IRS) * 4;
+    return ((size_t)F * MLP_H + MLP_H * MLP_H + 3 * MLP_H + (size_t)(F > MLP_H ? F : MLP_H) * IRS) * 4;
 }
 
 cudaError_t forward(const float* params, int F, const float* feat, int m, float* out, cudaStream_t st) {

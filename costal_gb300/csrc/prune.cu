@@ -93,50 +93,76 @@ __global__ void __launch_bounds__(KM_BLOCK) k_assign(const float* __restrict__ r
     assign[i] = arg;
 }
 
-// One CTA per centroid: the normalised sum of its rows. Thread t adds rows 4t … 4t+3, then 512 on,
-// in order, then the 128 partial sums are combined by a fixed tree: deterministic. An empty cluster keeps its
-// previous centroid.
-constexpr int UPD_T = 128;
+// One CTA per centroid: the normalised sum of its rows, summed in a fixed order (deterministic): the
+// rows fall into 128 classes by (row / 4) mod 128, each class adds its rows in row order, and the 128
+// class sums are combined by a fixed pairwise tree. Warp w takes classes 16w … 16w+15 one after the
+// other, lane t holding dimensions t and t + 32: the class's assignment words are loaded four per
+// lane at once and its matches found by ballots, so the warp's branches are uniform and a row is read
+// coalesced. An empty cluster keeps its previous centroid.
+constexpr int UPD_T = 256;
+constexpr int UPD_CLASSES = 128;
+constexpr int UPD_GROUPS = 128;  // word groups of a class: m ≤ 4 · 128 · 128 rows
+static_assert(4 * UPD_CLASSES * UPD_GROUPS >= SAMPLE, "the centroid update covers the k-means sample");
 __global__ void __launch_bounds__(UPD_T) k_centroid_update(const float* __restrict__ rows, int m, int d,
                                                            const uint32_t* __restrict__ assign, float* __restrict__ cent) {
-    __shared__ float part[UPD_T][65];
-    __shared__ int cnt_s[UPD_T];
-    const int c = blockIdx.x;
-    float acc[64];
-#pragma unroll
-    for (int t = 0; t < 64; ++t) acc[t] = 0.0f;
-    int cnt = 0;
-    auto add_row = [&](int i) {
-        ++cnt;
-#pragma unroll
-        for (int t = 0; t < 64; ++t)
-            if (t < d) acc[t] += rows[(size_t)i * d + t];
-    };
-    // four assignments per 16-byte load (the array is 256-byte aligned), then the tail
+    constexpr int NW = UPD_T / 32, CPW = UPD_CLASSES / NW;
+    __shared__ float part[UPD_CLASSES][65];
+    __shared__ int cnt_s[UPD_CLASSES];
+    __shared__ float nrm;
+    const int c = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m4 = m & ~3;
-    for (int i4 = 4 * threadIdx.x; i4 < m4; i4 += 4 * UPD_T) {
-        const uint4 a = *reinterpret_cast<const uint4*>(assign + i4);
-        if (a.x == (uint32_t)c) add_row(i4);
-        if (a.y == (uint32_t)c) add_row(i4 + 1);
-        if (a.z == (uint32_t)c) add_row(i4 + 2);
-        if (a.w == (uint32_t)c) add_row(i4 + 3);
-    }
-    for (int i = m4 + threadIdx.x; i < m; i += UPD_T)
-        if (assign[i] == (uint32_t)c) add_row(i);
+    for (int k = 0; k < CPW; ++k) {
+        const int cls = warp * CPW + k;
+        float s0 = 0.0f, s1 = 0.0f;
+        int cnt = 0;
+        auto add_row = [&](int i) {
+            ++cnt;
+            if (lane < d) s0 += rows[(size_t)i * d + lane];
+            if (lane + 32 < d) s1 += rows[(size_t)i * d + lane + 32];
+        };
+        // the class's word groups q = 0 … 127 (rows 4·cls + 512·q …+3), four per lane, all loaded at
+        // once; then the matches are added in row order: group by group (ballot, lowest lane first)
+        // and within a group by row
+        uint32_t mask[UPD_GROUPS / 32];
 #pragma unroll
-    for (int t = 0; t < 64; ++t)
-        if (t < d) part[threadIdx.x][t] = acc[t];
-    cnt_s[threadIdx.x] = cnt;
-    __syncthreads();
-    for (int s = UPD_T / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) {
-            for (int t = 0; t < d; ++t) part[threadIdx.x][t] += part[threadIdx.x + s][t];
-            cnt_s[threadIdx.x] += cnt_s[threadIdx.x + s];
+        for (int r = 0; r < UPD_GROUPS / 32; ++r) {
+            const int i4 = 4 * cls + 4 * UPD_CLASSES * (r * 32 + lane);
+            mask[r] = 0u;
+            if (i4 < m4) {
+                const uint4 a = *reinterpret_cast<const uint4*>(assign + i4);  // (the array is 256-byte aligned)
+                mask[r] = (a.x == (uint32_t)c ? 1u : 0u) | (a.y == (uint32_t)c ? 2u : 0u) |
+                          (a.z == (uint32_t)c ? 4u : 0u) | (a.w == (uint32_t)c ? 8u : 0u);
+            }
         }
+#pragma unroll
+        for (int r = 0; r < UPD_GROUPS / 32; ++r) {
+            unsigned any = __ballot_sync(COSTAL_FULL_MASK, mask[r] != 0u);
+            while (any) {
+                const int L = __ffs(any) - 1;
+                any &= any - 1;
+                unsigned mk = __shfl_sync(COSTAL_FULL_MASK, mask[r], L);
+                const int i4 = 4 * cls + 4 * UPD_CLASSES * (r * 32 + L);
+                while (mk) {
+                    add_row(i4 + __ffs(mk) - 1);
+                    mk &= mk - 1;
+                }
+            }
+        }
+        if (m4 + cls < m && assign[m4 + cls] == (uint32_t)c) add_row(m4 + cls);  // the last m mod 4 rows
+        if (lane < d) part[cls][lane] = s0;
+        if (lane + 32 < d) part[cls][lane + 32] = s1;
+        if (lane == 0) cnt_s[cls] = cnt;
+    }
+    __syncthreads();
+    for (int s = UPD_CLASSES / 2; s > 0; s >>= 1) {
+        for (int e = threadIdx.x; e < s * d; e += UPD_T) {
+            const int cls = e / d, t = e - cls * d;
+            part[cls][t] += part[cls + s][t];
+        }
+        if ((int)threadIdx.x < s) cnt_s[threadIdx.x] += cnt_s[threadIdx.x + s];
         __syncthreads();
     }
     if (cnt_s[0] == 0) return;
-    __shared__ float nrm;
     if (threadIdx.x == 0) {
         double nn = 0.0;
         for (int t = 0; t < d; ++t) nn += (double)part[0][t] * part[0][t];
@@ -587,7 +613,6 @@ struct Scratch {
     uint32_t* hist;
     uint32_t* cell_start;
     uint32_t* sample_idx;
-    float* wrows;  // [n][d] the normalised rows in working order
 };
 
 __global__ void k_sample_idx(uint32_t* idx, int m, int n) {
@@ -643,7 +668,7 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     S.hist = reinterpret_cast<uint32_t*>(take((size_t)nch * K * 4));
     S.cell_start = reinterpret_cast<uint32_t*>(take((size_t)(K + 1) * 4));
     S.sample_idx = reinterpret_cast<uint32_t*>(take((size_t)m * 4));
-    S.wrows = reinterpret_cast<float*>(take((size_t)n * d * 4));
+    P.wrows = reinterpret_cast<float*>(take((size_t)n * d * 4));
     P.scratch = S.sample_rows;
 
     const size_t csm = (size_t)K * ((d + 3) & ~3) * 4;
@@ -662,9 +687,9 @@ cudaError_t build_order(void* ws, const float* xsT, int n, int np, int d, cudaSt
     k_cell_scan<<<1, K, 0, st>>>(S.hist, nch, K, S.cell_start); note_launch();
     k_cell_scatter<<<(nch + 127) / 128, 128, 0, st>>>(P.cell, n, K, S.hist, P.perm); note_launch();
     // the rows in working order, row-major, for the block geometry's contiguous reads
-    k_gather_rows<<<std::min((n * d + 255) / 256, 8 * 1024), 256, 0, st>>>(xsT, np, d, P.perm, n, S.wrows); note_launch();
-    k_block_geom<<<nqb, 256, 0, st>>>(S.wrows, d, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
-    k_block_geom<<<ncb, 256, 0, st>>>(S.wrows, d, n, cb, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f); note_launch();
+    k_gather_rows<<<std::min((n * d + 255) / 256, 8 * 1024), 256, 0, st>>>(xsT, np, d, P.perm, n, P.wrows); note_launch();
+    k_block_geom<<<nqb, 256, 0, st>>>(P.wrows, d, n, QB, P.qcenter, P.qradius, nullptr, nullptr); note_launch();
+    k_block_geom<<<ncb, 256, 0, st>>>(P.wrows, d, n, cb, P.ccenter, P.cradius, P.ccenter_f, P.cradius_f); note_launch();
     return cudaGetLastError();
 }
 

@@ -41,6 +41,7 @@ struct Plan {
     float* ub_skip;      // [nqb]
     double* row_ub;      // [n] (original order) pruning floor of the certificate
     float* tq;           // [nqb] per-query-block thresholds (NULL = keep every block)
+    float* wrows;        // [n][d] the normalised rows in working order, row-major
     const float* rowmax;    // [nqb][ncb] per-row bound data (tc::launch_rowmax), or NULL: cone bound only
     const float* rm_delta;  // its error margin (device scalar)
     void* scratch;       // k-means sample, histograms
