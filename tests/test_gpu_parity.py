@@ -160,8 +160,9 @@ def test_compact_operands_on_the_tensor_cores(ext, oracle, n, d, k, margin):
 @pytest.mark.parametrize("n,d,k,margin", [(700, 43, 10, None), (600, 300, 15, None), (500, 2000, 15, 15),
                                           (400, 130, 20, 40), (650, 41, 10, None), (640, 42, 12, 12)])
 def test_deep_rows_on_the_tensor_cores(ext, oracle, n, d, k, margin):
-    """Rows with 3d > 128 run the tensor-core K loop (no locality order); d = 41, 42 the resident
-    3d-wide form at its upper end: same exact output."""
+    """Rows with 3d > 128 run the tensor-core K loop (with the locality order, block lists and early
+    stop up to d = 64, in row order above); d = 41, 42 the resident 3d-wide form at its upper end: same
+    exact output."""
     rng = np.random.default_rng(n + d)
     means = rng.normal(0, 2, size=(9, d))
     x = np.arcsinh((means[rng.integers(0, 9, n)] + rng.normal(0, 0.6, size=(n, d))) / 5.0).astype(np.float32)
