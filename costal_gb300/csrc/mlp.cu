@@ -195,36 +195,54 @@ __device__ void forward_block(const float* __restrict__ P, int F, const float* _
 }
 
 // ---- inference ----------------------------------------------------------------------------------
-// Persistent CTAs of 256 threads: the weights, transposed, stay in shared memory while the CTA walks
-// 128-row tiles. Thread (ty, tx) = (tid / 16, tid % 16) holds an 8-row × 8-unit register tile: rows
-// 4ty … 4ty+3 and 64+4ty … 64+4ty+3, units 4tx … 4tx+3 and 64+4tx … 64+4tx+3, so that per input feature
-// two float4 of activations (the same for the 16 threads of a half-warp) and two float4 of weights (16
-// consecutive float4 across the half-warp: no bank conflicts) feed 64 FMAs. One buffer holds the tile's
-// features, transposed, and then its layer-1 activations. Every hidden unit's sum runs bias first,
-// then the inputs in order, like forward_block; the output adds the 16 threads' partial sums of 8 units
-// in a fixed tree.
-constexpr int IR = 128;       // rows per tile
-constexpr int IT = 256;       // threads
-constexpr int IRS = IR + 4;   // row stride of the transposed activations (float4-aligned)
+// On the tensor cores (mma.sync m16n8k16, bf16 operands, FP32 accumulation): the weights, rounded to
+// bf16, stay in shared memory ([unit][input], which is the MMA's column-major B) while persistent CTAs
+// of 8 warps walk 128-row tiles, 16 rows a warp. Layer 1 multiplies the tile's features (rounded to
+// bf16, row-major A in shared memory) by W1ᵀ into 16 accumulator fragments of 8 units; bias and ReLU
+// are applied in registers, and the fragments, rounded to bf16, are layer 2's A operand as they stand
+// (the accumulator layout of two adjacent 8-unit tiles is the A layout of one 16-wide K step), so the
+// activations never leave the registers. Layer 2 likewise; the output is the dot of ReLU(layer 2) with
+// w3 in FP32: each thread's 32 units, then the four threads of a row in a fixed tree, plus b3.
+// Padded inputs (K up to the next multiple of 16) and rows past m are zero.
+constexpr int IR = 128;           // rows per tile
+constexpr int IT = 256;           // threads (8 warps × 16 rows)
+constexpr int IKP = MLP_MAXF + 8;  // shared-memory row stride (bf16) of W1 and the features: conflict-free
+constexpr int IHP = MLP_H + 8;     // row stride of W2
 
-__global__ void __launch_bounds__(IT, 1) k_infer(const float* __restrict__ P, int F, const float* __restrict__ feat,
-                                                 int m, float* __restrict__ out) {
-    extern __shared__ __align__(16) float sm[];
-    float* w1t = sm;                            // [F][H]
-    float* w2t = w1t + (size_t)F * MLP_H;       // [H][H]
-    float* b1 = w2t + MLP_H * MLP_H;            // [H]
-    float* b2 = b1 + MLP_H;                     // [H]
-    float* w3 = b2 + MLP_H;                     // [H]
-    float* act = w3 + MLP_H;                    // [max(F, H)][IRS]: features, then layer-1 activations
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (low half), .y = hi
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(IT) k_infer(const float* __restrict__ P, int F, const float* __restrict__ feat,
+                                              int m, float* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_i[];
+    __nv_bfloat16* w1s = reinterpret_cast<__nv_bfloat16*>(smem_i);  // [H][IKP]
+    __nv_bfloat16* w2s = w1s + (size_t)MLP_H * IKP;                  // [H][IHP]
+    __nv_bfloat16* xs = w2s + (size_t)MLP_H * IHP;                   // [IR][IKP] the tile's features
+    float* b1 = reinterpret_cast<float*>(xs + (size_t)IR * IKP);     // [H]
+    float* b2 = b1 + MLP_H;                                          // [H]
+    float* w3 = b2 + MLP_H;                                          // [H]
     const Off o = offsets(F);
-    const int tid = threadIdx.x;
-    for (int e = tid; e < MLP_H * F; e += IT) {
-        const int u = e / F, t = e % F;
-        w1t[t * MLP_H + u] = P[o.w1 + e];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, tq = lane & 3;  // the fragment's row group and thread in group
+    const int KS1 = (F + 15) >> 4;           // layer-1 K steps
+    const int kp = KS1 * 16;
+    for (int e = tid; e < MLP_H * kp; e += IT) {
+        const int u = e / kp, t = e - u * kp;
+        w1s[u * IKP + t] = __float2bfloat16_rn(t < F ? P[o.w1 + (size_t)u * F + t] : 0.0f);
     }
     for (int e = tid; e < MLP_H * MLP_H; e += IT) {
-        const int u = e / MLP_H, t = e % MLP_H;
-        w2t[t * MLP_H + u] = P[o.w2 + e];
+        const int u = e / MLP_H, t = e - u * MLP_H;
+        w2s[u * IHP + t] = __float2bfloat16_rn(P[o.w2 + e]);
     }
     if (tid < MLP_H) {
         b1[tid] = P[o.b1 + tid];
@@ -232,72 +250,79 @@ __global__ void __launch_bounds__(IT, 1) k_infer(const float* __restrict__ P, in
         w3[tid] = P[o.w3 + tid];
     }
     const float b3 = P[o.b3];
-    const int ty = tid >> 4, tx = tid & 15;
-    const int ra = 4 * ty, rb = 64 + 4 * ty;  // the thread's two groups of 4 rows
-    const int ua = 4 * tx, ub = 64 + 4 * tx;  // and of 4 units
     const int ntiles = (m + IR - 1) / IR;
-    float acc[8][8];
-    // one layer: acc[i][j] = bias(unit j) + Σ_t w(t, unit j)·x(t, row i), t in order
-    auto layer = [&](const float* wt, const float* bias, int K) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float b = bias[j < 4 ? ua + j : ub + j - 4];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) acc[i][j] = b;
-        }
-        for (int t = 0; t < K; ++t) {
-            const float4 a0 = *reinterpret_cast<const float4*>(act + t * IRS + ra);
-            const float4 a1 = *reinterpret_cast<const float4*>(act + t * IRS + rb);
-            const float4 w0 = *reinterpret_cast<const float4*>(wt + t * MLP_H + ua);
-            const float4 w1 = *reinterpret_cast<const float4*>(wt + t * MLP_H + ub);
-            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(wv[j], av[i], acc[i][j]);
-        }
-    };
+    const int r_w = warp * 16;  // the warp's first row in the tile
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r0 = tile * IR;
-        __syncthreads();  // the previous tile's readers of act are done (and the weights loaded)
-        // the tile's features, read row by row (coalesced) and stored transposed
-        for (int e = tid; e < IR * F; e += IT) {
-            const int r = e / F, t = e - r * F;
-            act[t * IRS + r] = r0 + r < m ? feat[(size_t)(r0 + r) * F + t] : 0.0f;
+        __syncthreads();  // the previous tile's readers of xs are done (and the weights loaded)
+        for (int e = tid; e < IR * kp; e += IT) {
+            const int r = e / kp, t = e - r * kp;
+            xs[r * IKP + t] = __float2bfloat16_rn(r0 + r < m && t < F ? feat[(size_t)(r0 + r) * F + t] : 0.0f);
         }
         __syncthreads();
-        layer(w1t, b1, F);
-        __syncthreads();  // every thread has read the features: act now takes the layer-1 activations
+        // layer 1: acc[j] = the 16 rows × units 8j … 8j+7
+        float acc[16][4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int u = j < 4 ? ua + j : ub + j - 4;
-            *reinterpret_cast<float4*>(act + u * IRS + ra) = make_float4(
-                fmaxf(acc[0][j], 0.0f), fmaxf(acc[1][j], 0.0f), fmaxf(acc[2][j], 0.0f), fmaxf(acc[3][j], 0.0f));
-            *reinterpret_cast<float4*>(act + u * IRS + rb) = make_float4(
-                fmaxf(acc[4][j], 0.0f), fmaxf(acc[5][j], 0.0f), fmaxf(acc[6][j], 0.0f), fmaxf(acc[7][j], 0.0f));
-        }
-        __syncthreads();
-        layer(w2t, b2, MLP_H);
-        // output layer: each thread's 8 units, then the 16 threads of a row group in a fixed tree
-        float p[8];
+        for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        for (int ks = 0; ks < KS1; ++ks) {
+            const int k0 = ks * 16 + 2 * tq;
+            uint32_t a[4];
+            a[0] = *reinterpret_cast<const uint32_t*>(xs + (r_w + g) * IKP + k0);
+            a[1] = *reinterpret_cast<const uint32_t*>(xs + (r_w + g + 8) * IKP + k0);
+            a[2] = *reinterpret_cast<const uint32_t*>(xs + (r_w + g) * IKP + k0 + 8);
+            a[3] = *reinterpret_cast<const uint32_t*>(xs + (r_w + g + 8) * IKP + k0 + 8);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            float z = 0.0f;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) z = fmaf(w3[j < 4 ? ua + j : ub + j - 4], fmaxf(acc[i][j], 0.0f), z);
-            p[i] = z;
-        }
-#pragma unroll
-        for (int off = 1; off < 16; off <<= 1)
-#pragma unroll
-            for (int i = 0; i < 8; ++i) p[i] += __shfl_xor_sync(COSTAL_FULL_MASK, p[i], off);
-        if (tx == 0) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int r = r0 + (i < 4 ? ra + i : rb + i - 4);
-                if (r < m) out[r] = b3 + p[i];
+            for (int j = 0; j < 16; ++j) {
+                const __nv_bfloat16* wr = w1s + (8 * j + g) * IKP + k0;
+                mma_bf16_16816(acc[j], a, *reinterpret_cast<const uint32_t*>(wr),
+                               *reinterpret_cast<const uint32_t*>(wr + 8));
             }
+        }
+        // bias + ReLU, rounded to bf16: layer 2's A fragments (K step s = units 16s … 16s+15)
+        uint32_t h[8][4];
+#pragma unroll
+        for (int s2 = 0; s2 < 8; ++s2) {
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int j = 2 * s2 + half, u = 8 * j + 2 * tq;
+                const float bu = b1[u], bv = b1[u + 1];
+                h[s2][2 * half] = pack_bf16(fmaxf(acc[j][0] + bu, 0.0f), fmaxf(acc[j][1] + bv, 0.0f));
+                h[s2][2 * half + 1] = pack_bf16(fmaxf(acc[j][2] + bu, 0.0f), fmaxf(acc[j][3] + bv, 0.0f));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+#pragma unroll
+        for (int s2 = 0; s2 < 8; ++s2) {
+            // A fragment order: (row g, k lo), (row g + 8, k lo), (row g, k hi), (row g + 8, k hi)
+            const uint32_t a[4] = {h[s2][0], h[s2][1], h[s2][2], h[s2][3]};
+            const int k0 = s2 * 16 + 2 * tq;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const __nv_bfloat16* wr = w2s + (8 * j + g) * IHP + k0;
+                mma_bf16_16816(acc[j], a, *reinterpret_cast<const uint32_t*>(wr),
+                               *reinterpret_cast<const uint32_t*>(wr + 8));
+            }
+        }
+        // output: Σ_u w3[u]·ReLU(layer 2 + b2) for rows g and g + 8, units 8j + 2tq, 8j + 2tq + 1
+        float pg = 0.0f, pg8 = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int u = 8 * j + 2 * tq;
+            pg = fmaf(w3[u], fmaxf(acc[j][0] + b2[u], 0.0f), pg);
+            pg = fmaf(w3[u + 1], fmaxf(acc[j][1] + b2[u + 1], 0.0f), pg);
+            pg8 = fmaf(w3[u], fmaxf(acc[j][2] + b2[u], 0.0f), pg8);
+            pg8 = fmaf(w3[u + 1], fmaxf(acc[j][3] + b2[u + 1], 0.0f), pg8);
+        }
+#pragma unroll
+        for (int off = 1; off < 4; off <<= 1) {
+            pg += __shfl_xor_sync(COSTAL_FULL_MASK, pg, off);
+            pg8 += __shfl_xor_sync(COSTAL_FULL_MASK, pg8, off);
+        }
+        if (tq == 0) {
+            const int r = r0 + r_w + g;
+            if (r < m) out[r] = b3 + pg;
+            if (r + 8 < m) out[r + 8] = b3 + pg8;
         }
     }
 }
@@ -431,7 +456,8 @@ cudaError_t features(const float* xsT, int np, int d, const float* centroids, in
 }
 
 static size_t infer_smem(int F) {
-    return ((size_t)F * MLP_H + MLP_H * MLP_H + 3 * MLP_H + (size_t)(F > MLP_H ? F : MLP_H) * IRS) * 4;
+    (void)F;
+    return ((size_t)MLP_H * IKP + (size_t)MLP_H * IHP + (size_t)IR * IKP) * 2 + 3 * MLP_H * 4;
 }
 
 cudaError_t forward(const float* params, int F, const float* feat, int m, float* out, cudaStream_t st) {
@@ -443,7 +469,7 @@ cudaError_t forward(const float* params, int F, const float* feat, int m, float*
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     const int tiles = (m + IR - 1) / IR;
-    k_infer<<<tiles < sms ? tiles : sms, IT, smem, st>>>(params, F, feat, m, out); note_launch();
+    k_infer<<<tiles < 2 * sms ? tiles : 2 * sms, IT, smem, st>>>(params, F, feat, m, out); note_launch();
     return cudaGetLastError();
 }
 
