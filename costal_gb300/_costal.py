@@ -443,7 +443,8 @@ def _mlp_clear():
 
 
 def _mlp_forward(params, feat):
-    """Test hook: the GPU forward pass for given weights and features (m, F)."""
+    """Test hook: the GPU inference pass (bf16 operands on the tensor cores, FP32 accumulation) for given
+    weights and features (m, F)."""
     params = np.ascontiguousarray(params, dtype=np.float32)
     feat = np.ascontiguousarray(feat, dtype=np.float32)
     m, F = feat.shape

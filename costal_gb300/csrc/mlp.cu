@@ -6,8 +6,9 @@
 // Training (costal_mlp_train) uses the pinball loss at a low quantile, so the prediction sits below
 // the true k-th score for most rows: it only sets a skip threshold, and every skip is certified
 // after the fact (a query whose k-th score does not beat its skipped blocks' bound is rescanned).
-// Inference runs in FP32 on bf16-rounded weights. Gradients are summed over fixed 32-row groups and
-// then over the groups in order, so training is deterministic.
+// Training runs the FP32 forward of that definition; inference runs on the tensor cores with bf16
+// operands (weights, features and first-layer activations) and FP32 accumulation. Gradients are
+// summed over fixed 32-row groups and then over the groups in order, so training is deterministic.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -30,7 +30,8 @@ namespace mlp {
 // Features of the rows `rows` (original indices; NULL = 0..m-1) from xsT and the unit centroids.
 cudaError_t features(const float* xsT, int np, int d, const float* centroids, int K, const uint32_t* rows, int m,
                      float* feat, cudaStream_t st);
-// Forward pass of m rows with the given parameter block: out[i].
+// Inference of m rows with the given parameter block: out[i] (tensor cores: bf16 weights, features and
+// first-layer activations, FP32 accumulation).
 cudaError_t forward(const float* params, int F, const float* feat, int m, float* out, cudaStream_t st);
 // Loss gradient (pinball loss at `quantile`, mean over the m rows) with respect to every
 // parameter, summed in a fixed order: grad[nparams]. `partial` holds ⌈m/32⌉ × nparams floats.

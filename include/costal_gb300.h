@@ -200,7 +200,8 @@ int costal_mlp_get(float* params, uint64_t capacity, uint64_t* count, uint32_t* 
 int costal_mlp_set(const float* params, uint64_t count, uint32_t d, uint32_t k, float quantile, char* err,
                    size_t errlen);
 int costal_mlp_clear(char* err, size_t errlen);
-/* Test hooks: the forward pass and the loss gradient for given weights and features (host buffers). */
+/* Test hooks: the inference pass (bf16 operands on the tensor cores, FP32 accumulation) and the loss
+ * gradient (FP32) for given weights and features (host buffers). */
 int costal_mlp_forward(const float* params, uint32_t F, const float* feat, uint64_t m, float* out, char* err,
                        size_t errlen);
 int costal_mlp_gradient(const float* params, uint32_t F, const float* feat, const float* y, uint64_t m,
