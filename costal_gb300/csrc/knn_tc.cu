@@ -1369,7 +1369,7 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
                           int sm_count, cudaStream_t st, int qb0, int qb1) {
     (void)sm_count;
     if (lists && list_cb != HALF_N && list_cb != BLOCK_N) return cudaErrorInvalidValue;
-    const int epc = lists && list_cb == HALF_N ? 2 : 1;  // list entries per tile
+    const bool pair = lists && list_cb == HALF_N;  // two list entries per tile
     CUtensorMap ma, mb, mbw;  // the column operand in boxes of one half tile and of a whole tile
     if (!make_map(&ma, plan.ops_a, plan.kpa, plan.np, BLOCK_M, plan.fp8) ||
         !make_map(&mb, plan.ops_b, plan.kpb, plan.np, HALF_N, plan.fp8) ||
@@ -1384,7 +1384,6 @@ cudaError_t launch_coarse(const Plan& plan, int cap, const uint32_t* lists, cons
     const int qblocks = (plan.n + BLOCK_M - 1) / BLOCK_M;
     if (qb1 < 0) qb1 = qblocks;
     if (qb0 < 0 || qb1 > qblocks || qb0 >= qb1) return cudaErrorInvalidValue;
-    const bool pair = epc == 2;
     auto kern = plan.fp8 ? (cap <= 32 ? k_coarse_tc<1, true, true> : k_coarse_tc<2, true, true>)
                 : !sh.resident ? (pair ? (cap <= 32 ? k_coarse_tc<1, true, false, true> : k_coarse_tc<2, true, false, true>)
                                        : (cap <= 32 ? k_coarse_tc<1, true> : k_coarse_tc<2, true>))
