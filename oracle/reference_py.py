@@ -1,8 +1,8 @@
 """TEST INFRASTRUCTURE ONLY — where the reference's own Python package and tests are, when present.
 
 The reference (ike12th/CosTaL 2.1.0) keeps its pure-Python package in `python/costal/` and its Python
-tests in `tests/`. This recipe finds that checkout: `$COSTAL_REFERENCE` if set, else the read-only
-copy at /root/reference that this build's container holds. Nothing is copied out of it: the
+tests in `tests/`. This recipe finds that checkout: `$COSTAL_REFERENCE` if set, else a read-only
+copy at /root/reference where the fixtures are recorded. Nothing is copied out of it: the
 reference package is imported from where it lies, only by tests/golden/make_dropin.py (which records
 what that package asks of `costal._costal`) and the CPU test that re-runs it. On a machine without
 the reference, `locate()` returns None and those skip.
